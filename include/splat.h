@@ -1,0 +1,202 @@
+/*
+ * splat.h -- C ABI of libsplat, the GB300 (sm_103a) Gaussian-splatting render
+ * path that stands in for jaxsplat's native module.
+ *
+ * Two families of entry points:
+ *
+ *  1. splat_xla_*: the reference's XLA custom-call targets, with the same
+ *     signature, buffer order and 80-byte opaque descriptor.  They replace
+ *     the four PyCapsules that jaxsplat registers at import
+ *     (lib/ffi.cu:4-13 registrations(), lib/ops.h:45-92):
+ *         void fn(cudaStream_t, void **buffers, const char *opaque, size_t len)
+ *     Like the reference they read the intersection count back to the host
+ *     and take their temporaries from the stream-ordered allocator
+ *     (cudaMallocAsync); unlike it they never synchronise the stream
+ *     otherwise, never throw, and record failures for splat_last_error().
+ *
+ *  2. splat_*: typed entry points with plain pointers, sizes, an explicit
+ *     stream, caller-provided workspace (size from the *_workspace_size
+ *     query) and an int status.  No allocation, no host synchronisation
+ *     (except splat_read_counts, which exists to read the count).
+ *
+ * All arrays are row-major, C-contiguous, fp32 unless marked, with the
+ * reference's shapes (jaxsplat/_project/abstract.py:7-77,
+ * jaxsplat/_rasterize/abstract.py:7-85).  N = num_points, I = number of
+ * tile/Gaussian intersections, T = tiles_x * tiles_y with
+ * tiles_x = ceil(W / block_width), tiles_y = ceil(H / block_width).
+ */
+#ifndef SPLAT_H_
+#define SPLAT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SPLAT_API __attribute__((visibility("default")))
+#else
+#define SPLAT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *splat_stream_t; /* == cudaStream_t */
+
+/* Status codes returned by every typed entry point. */
+enum {
+    SPLAT_OK = 0,
+    SPLAT_ERR_INVALID_ARG = 1, /* bad size, shape, pointer or block width */
+    SPLAT_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+    SPLAT_ERR_WORKSPACE = 3,   /* workspace smaller than *_workspace_size() */
+    SPLAT_ERR_OVERFLOW = 4,    /* intersection count exceeds the supported range */
+    SPLAT_ERR_DEVICE = 5       /* a device-side check fired (see splat_device_status_string) */
+};
+
+/*
+ * Render parameters: the fields of ops::Descriptor (lib/ops.h:9-22) that
+ * carry meaning, plus two controls of this library.
+ *   block_width   tile side in pixels, 2..16 (the reference's limit:
+ *                 block_width^2 <= MAX_GRID_DIM = 256, lib/common.h:9)
+ *   device_status optional device pointer to one uint32 that kernels OR
+ *                 failure bits into (NULL: checks still skip bad writes,
+ *                 nothing is recorded)
+ *   spin_limit    polls before a decoupled look-back wait gives up
+ *                 (0 = default)
+ */
+typedef struct splat_params {
+    uint32_t num_points;
+    uint32_t img_height;
+    uint32_t img_width;
+    float fx, fy, cx, cy;
+    float glob_scale;
+    float clip_thresh;
+    uint32_t block_width;
+    uint32_t *device_status;
+    uint32_t spin_limit;
+} splat_params;
+
+/* Thread-local message for the last failure in this thread. */
+SPLAT_API const char *splat_last_error(void);
+SPLAT_API const char *splat_status_string(int status);
+/* Text for the bits of a device status word. */
+SPLAT_API const char *splat_device_status_string(uint32_t bits);
+SPLAT_API int splat_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* Projection forward.  Replaces ops::project::fwd::xla (lib/ops.cu:12-61):
+ * project_gaussians_fwd (lib/kernels/forward.cu:13-131) fused with the int32
+ * inclusive scan of num_tiles_hit (lib/ops.cu:607-643) in one single-pass
+ * kernel.  Every output element is written (zeros where the reference's
+ * memsets leave zeros).
+ *   means3d (N,3) scales (N,3) quats (N,4, w-x-y-z) viewmat (4,4)
+ *   -> cov3d (N,6) xys (N,2) depths (N,1) radii (N,1) int32 conics (N,3)
+ *      compensation (N,1) num_tiles_hit (N,1) int32 cum_tiles_hit (N,1) int32
+ * total_out (optional, device int64): I as a 64-bit count. */
+SPLAT_API size_t splat_project_fwd_workspace_size(const splat_params *p);
+SPLAT_API int splat_project_fwd(const splat_params *p, const float *means3d, const float *scales,
+                      const float *quats, const float *viewmat, float *cov3d, float *xys,
+                      float *depths, int32_t *radii, float *conics, float *compensation,
+                      int32_t *num_tiles_hit, int32_t *cum_tiles_hit, int64_t *total_out,
+                      void *workspace, size_t workspace_bytes, splat_stream_t stream);
+
+/* Blocking read of the intersection count and, when status_dev is not NULL,
+ * of the device status word (which is then cleared).  Replaces the D2H read
+ * in lib/ops.cu:424-432.  total_dev: the int64 written by splat_project_fwd;
+ * when NULL, cum_tiles_hit[N-1] is read instead. */
+SPLAT_API int splat_read_counts(const splat_params *p, const int32_t *cum_tiles_hit,
+                      const int64_t *total_dev, uint32_t *status_dev, int64_t *num_intersects,
+                      uint32_t *status_out, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Sort and bin.  Replaces ops::sort_and_bin (lib/ops.cu:645-793): key
+ * emission (lib/kernels/forward.cu:135-179), a stable LSD radix sort of the
+ * 64-bit tile|depth keys over bits [0, 32+msb) (CUB SortPairs at
+ * lib/ops.cu:728-757; here an in-house onesweep sort) and the tile bin edges
+ * (lib/kernels/forward.cu:184-208).
+ *   -> gaussian_ids_sorted (I,) int32, tile_bins (T,2) int32 (empty tiles (0,0))
+ *   isect_ids / gaussian_ids (optional, may be NULL): the unsorted emission
+ *   isect_ids_sorted (optional, may be NULL): the sorted keys */
+SPLAT_API size_t splat_sort_workspace_size(const splat_params *p, int64_t num_intersects);
+SPLAT_API int splat_sort_and_bin(const splat_params *p, int64_t num_intersects, const float *xys,
+                       const float *depths, const int32_t *radii, const int32_t *cum_tiles_hit,
+                       int32_t *gaussian_ids_sorted, int32_t *tile_bins, int64_t *isect_ids,
+                       int32_t *gaussian_ids, int64_t *isect_ids_sorted, void *workspace,
+                       size_t workspace_bytes, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Rasterize forward over a sorted list.  Replaces the rasterize_fwd launch of
+ * ops::rasterize::fwd::xla (lib/ops.cu:144-160, kernel
+ * lib/kernels/forward.cu:339-462), including the empty-list path
+ * (lib/ops.cu:119-127: image = background, final_Ts = final_idx = 0).
+ *   colors (N,3) opacities (N,1) background (3,) xys (N,2) conics (N,3)
+ *   -> final_Ts (H,W,1) final_idx (H,W,1) int32 out_img (H,W,3) */
+SPLAT_API int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects,
+                        const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                        const float *xys, const float *conics, const float *colors,
+                        const float *opacities, const float *background, float *final_Ts,
+                        int32_t *final_idx, float *out_img, splat_stream_t stream);
+
+/* Rasterize backward over the same sorted list (no re-sort).  Replaces the
+ * rasterize_bwd launch of ops::rasterize::bwd::xla (lib/ops.cu:203-225,
+ * kernel lib/kernels/backward.cu:153-343).  Outputs are overwritten.
+ *   v_img (H,W,3) v_img_alpha (H,W,1)
+ *   -> v_colors (N,3) v_opacity (N,1) v_xy (N,2) v_conic (N,3)
+ *      v_xy_abs (N,2) optional: NULL skips the sum of |v_xy| that the
+ *      reference computes and jaxsplat discards. */
+SPLAT_API int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
+                        const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                        const float *xys, const float *conics, const float *colors,
+                        const float *opacities, const float *background, const float *final_Ts,
+                        const int32_t *final_idx, const float *v_img, const float *v_img_alpha,
+                        float *v_colors, float *v_opacity, float *v_xy, float *v_xy_abs,
+                        float *v_conic, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Projection backward.  Replaces ops::project::bwd::xla (lib/ops.cu:63-105,
+ * kernel lib/kernels/backward.cu:345-418).  Outputs are overwritten.
+ *   -> v_mean3d (N,3) v_scale (N,3) v_quat (N,4) v_cov2d (N,3) v_cov3d (N,6) */
+SPLAT_API int splat_project_bwd(const splat_params *p, const float *means3d, const float *scales,
+                      const float *quats, const float *viewmat, const float *cov3d,
+                      const int32_t *radii, const float *conics, const float *compensation,
+                      const float *v_xy, const float *v_depth, const float *v_conic,
+                      const float *v_compensation, float *v_mean3d, float *v_scale,
+                      float *v_quat, float *v_cov2d, float *v_cov3d, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Mean squared error against a target and its cotangent:
+ * loss_out[0] = mean((img - target)^2), v_img = 2 (img - target) / count.
+ * loss_out is overwritten.  (The loss of the reference's fitting example,
+ * examples/single_image.py:26-29, used by the benchmark step.) */
+SPLAT_API int splat_l2_loss(const float *img, const float *target, int64_t count, float *loss_out,
+                  float *v_img, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Legacy XLA custom-call targets (drop-in for lib/ffi.cu:4-13).  Buffers in
+ * the order of jaxsplat/_{project,rasterize}/lowering.py; opaque is the
+ * 80-byte descriptor of splat_xla_make_descriptor (lib/ffi.cu:15-52). */
+SPLAT_API void splat_xla_project_fwd(splat_stream_t stream, void **buffers, const char *opaque,
+                           size_t opaque_len);
+SPLAT_API void splat_xla_project_bwd(splat_stream_t stream, void **buffers, const char *opaque,
+                           size_t opaque_len);
+SPLAT_API void splat_xla_rasterize_fwd(splat_stream_t stream, void **buffers, const char *opaque,
+                             size_t opaque_len);
+SPLAT_API void splat_xla_rasterize_bwd(splat_stream_t stream, void **buffers, const char *opaque,
+                             size_t opaque_len);
+/* img_shape is (H, W) as in jaxsplat; writes 80 bytes to out. */
+SPLAT_API int splat_xla_make_descriptor(uint32_t num_points, uint32_t img_h, uint32_t img_w, float fx,
+                              float fy, float cx, float cy, float glob_scale, float clip_thresh,
+                              uint32_t block_width, void *out, size_t out_len);
+
+/* ---------------------------------------------------------------------- */
+/* Self-test of the bounded wait: one block waits on a flag that nothing
+ * sets, with `limit` polls, then records DEV_LOOKBACK_TIMEOUT in *status_dev
+ * (device uint32) and returns.  Exists so the timeout path can be exercised
+ * without hanging a GPU. */
+SPLAT_API int splat_selftest_wait_timeout(uint32_t limit, uint32_t *status_dev, splat_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPLAT_H_ */

@@ -1,0 +1,93 @@
+"""The C ABI library loads, exports every symbol include/splat.h declares,
+and its plain-data layouts match the header and the reference's descriptor.
+No kernel is launched here (no GPU needed)."""
+
+import ctypes as C
+import os
+import re
+import struct
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "splat.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from jaxsplat_gb300 import _lib
+    from jaxsplat_gb300.build import build
+
+    build()
+    return _lib.load()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(splat_\w+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+    from jaxsplat_gb300 import _lib
+
+    assert sorted(_lib.EXPORTED) == names
+
+
+def test_params_layout_matches_header(tmp_path):
+    from jaxsplat_gb300._lib import SplatParams
+
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "splat.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu\\n\", sizeof(splat_params),"
+        " offsetof(splat_params, block_width), offsetof(splat_params, device_status),"
+        " offsetof(splat_params, spin_limit)); return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    size, bw, ds, sl = map(int, subprocess.check_output([str(exe)]).split())
+    assert C.sizeof(SplatParams) == size
+    assert SplatParams.block_width.offset == bw
+    assert SplatParams.device_status.offset == ds
+    assert SplatParams.spin_limit.offset == sl
+
+
+def test_descriptor_matches_reference_layout(lib):
+    """splat_xla_make_descriptor writes the 80 bytes that jaxsplat's
+    make_descriptor packs (lib/ffi.cu:15-52, struct lib/ops.h:9-22)."""
+    buf = C.create_string_buffer(80)
+    rc = lib.splat_xla_make_descriptor(100_000, 1080, 1920, 1200.0, 1100.0, 960.0, 540.0, 1.0,
+                                       0.01, 16, buf, 80)
+    assert rc == 0
+    want = struct.pack("<I3I4f", 100_000, 1920, 1080, 1, 1200.0, 1100.0, 960.0, 540.0)
+    want += struct.pack("<ffII I3I3I", 1.0, 0.01, 16, 391, 256, 120, 68, 1, 16, 16, 1)
+    want += b"\0" * (80 - len(want))
+    assert buf.raw == want
+
+
+def test_descriptor_size_is_checked(lib):
+    buf = C.create_string_buffer(40)
+    assert lib.splat_xla_make_descriptor(1, 1, 1, 1.0, 1.0, 0.0, 0.0, 1.0, 0.0, 16, buf, 40) == 1
+    assert b"80" in lib.splat_last_error()
+
+
+@pytest.mark.parametrize("bw", [0, 1, 17, 64])
+def test_invalid_block_width_rejected_without_gpu(lib, bw):
+    from jaxsplat_gb300 import _lib
+
+    p = _lib.make_params(10, (32, 32), block_width=bw)
+    rc = lib.splat_project_fwd(C.byref(p), *([None] * 13), None, 0, None)
+    assert rc == 1  # SPLAT_ERR_INVALID_ARG, before any CUDA call
+    assert b"block_width" in lib.splat_last_error()
+
+
+def test_strings(lib):
+    assert lib.splat_status_string(4) == b"intersection count out of range"
+    assert b"lookback-timeout" in lib.splat_device_status_string(1)
+    assert lib.splat_version() >= 1
