@@ -118,9 +118,9 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
 // Backward.
 
 // Sum of 8 values over the warp, transposed: on return lane L holds the
-// warp total of value (L >> 2) & 7.
-__device__ __forceinline__ float warp_sum8_transposed(float v[8]) {
-    const int lane = threadIdx.x & 31;
+// warp total of value (L >> 2) & 7.  `lane` is the caller's lane index (the
+// blocks here are two-dimensional, so threadIdx.x is not the lane).
+__device__ __forceinline__ float warp_sum8_transposed(const float v[8], int lane) {
     float b[4], c[2];
     const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
 #pragma unroll
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                 }
             }
             if (wmask == 0xffffffffu) {
-                const float s8 = warp_sum8_transposed(g8);
+                const float s8 = warp_sum8_transposed(g8, lane);
                 const float sop = warp_sum(g_op);
                 if ((lane & 3) == 0) atomicAdd(&s_acc[t][lane >> 2], s8);
                 if (lane == 0) {
