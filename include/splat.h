@@ -189,6 +189,31 @@ SPLAT_API int splat_xla_make_descriptor(uint32_t num_points, uint32_t img_h, uin
                               uint32_t block_width, void *out, size_t out_len);
 
 /* ---------------------------------------------------------------------- */
+/* Projection forward without a workspace (no counterpart in the reference).
+ * For callers that cannot allocate device memory -- e.g. a plugin inside a
+ * host application that owns and pools all device memory, or another
+ * runtime's handler where cudaMalloc would synchronise or is not allowed.
+ * Same inputs, outputs and results as splat_project_fwd; the scan's scratch
+ * is a fixed device array inside the library (about 0.5 MB per GPU that
+ * loads it, held until exit).
+ *   - at most 16,777,216 Gaussians; larger inputs fail with
+ *     SPLAT_ERR_INVALID_ARG before any GPU work;
+ *   - uses the calling thread's current device (the stream must belong to
+ *     it); the first call on a device looks up the array's device address,
+ *     so make that first call before any stream capture;
+ *   - all calls on a device share the array: calls that overlap on the GPU
+ *     race and must be ordered by the caller; each call clears the part it
+ *     uses, so back-to-back calls are fine;
+ *   - allocates nothing (no cudaMalloc/cudaFree, no allocator calls). */
+SPLAT_API int splat_project_fwd_noalloc(const splat_params *p, const float *means3d,
+                                        const float *scales, const float *quats,
+                                        const float *viewmat, float *cov3d, float *xys,
+                                        float *depths, int32_t *radii, float *conics,
+                                        float *compensation, int32_t *num_tiles_hit,
+                                        int32_t *cum_tiles_hit, int64_t *total_out,
+                                        splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Self-test of the bounded wait: one block waits on a flag that nothing
  * sets, with `limit` polls, then records DEV_LOOKBACK_TIMEOUT in *status_dev
  * (device uint32) and returns.  Exists so the timeout path can be exercised

@@ -66,6 +66,9 @@ static int validate(const splat_params *p) {
     return SPLAT_OK;
 }
 
+// Parameter validation shared with the other translation units.
+int check_params(const splat_params *p) { return validate(p); }
+
 static int check_count(long long count) {
     if (count < 0 || count > kMaxIntersects)
         return fail(SPLAT_ERR_OVERFLOW, "intersection count %lld outside [0, %lld]", count,
