@@ -115,70 +115,58 @@ class ClockSampler:
 # workloads
 
 class OursStep:
-    """The render path through libsplat's C ABI (jaxsplat_gb300._ops)."""
+    """The render path through libsplat's C ABI, as one preallocated,
+    sync-free step (jaxsplat_gb300.RenderSession) replayed as a CUDA graph."""
 
-    def __init__(self, sc, dev):
+    STAGES = ["project_fwd", "sort", "raster_fwd", "l2_loss", "raster_bwd", "project_bwd", "end"]
+
+    def __init__(self, sc, dev, graph=True):
         import torch
 
-        from jaxsplat_gb300 import _ops
+        from jaxsplat_gb300.session import RenderSession
 
-        self.torch, self.ops, self.sc, self.dev = torch, _ops, sc, dev
-        self.kw = dict(sc.kwargs, block_width=sc.spec.block_width)
-        self.rkw = dict(img_shape=self.kw["img_shape"], block_width=self.kw["block_width"])
+        self.torch, self.sc, self.dev = torch, sc, dev
+        kw = sc.kwargs
+        self.sess = RenderSession(sc.spec.num_points, img_shape=kw["img_shape"], f=kw["f"],
+                                  c=kw["c"], glob_scale=kw["glob_scale"],
+                                  clip_thresh=kw["clip_thresh"], block_size=sc.spec.block_width,
+                                  device=dev)
         self.host = {k: torch.from_numpy(getattr(sc, k)).pin_memory()
                      for k in ("means3d", "scales", "quats", "colors", "opacities", "viewmat",
                                "background", "target")}
-        self.d = {k: v.to(dev) for k, v in self.host.items()}
-        n = sc.spec.num_points
-        self.zn = torch.zeros(n, 1, device=dev)
-        h, w = self.kw["img_shape"]
-        self.zalpha = torch.zeros(h, w, 1, device=dev)
-        self.count = None
-        self.passes = None
+        self.upload()
+        self.count = self.sess.measure_capacity()
+        self.graph = graph
+        if graph:
+            self.sess.capture()
+        h, w = kw["img_shape"]
+        bw = sc.spec.block_width
+        tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
+        tile_passes = (max(1, (tiles - 1).bit_length()) + 7) // 8
+        # project, depth keys, 4-pass depth sort (+hist, offsets), emission,
+        # tile sort (+hist, offsets), bins, pack, raster fwd, loss, raster bwd,
+        # project bwd
+        self.kernels_per_step = 1 + 1 + 6 + 1 + (2 + tile_passes) + 1 + 1 + 1 + 1 + 1 + 1
+        self.passes = tile_passes
 
     def launches_per_step(self):
-        # project_fwd, emit, hist, offsets, passes x onesweep, tile_bins,
-        # raster_fwd, l2_loss, raster_bwd, project_bwd
-        return 9 + self.passes
+        return self.kernels_per_step
 
     def step(self, ev=None):
-        torch, ops, d, kw = self.torch, self.ops, self.d, self.kw
-        rec = (lambda name: ev[name].record()) if ev else (lambda name: None)
-        n = d["means3d"].shape[0]
-        rec("t0")
-        p = ops.project_fwd(d["means3d"], d["scales"], d["quats"], d["viewmat"], **kw)
-        rec("t1")
-        count = ops.read_counts(n, p["cum_tiles_hit"], p["total"], device=self.dev)
-        s = ops.sort_and_bin(count, p["xys"], p["depths"], p["radii"], p["cum_tiles_hit"],
-                             **self.rkw)
-        rec("t2")
-        r = ops.rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], p["xys"],
-                              p["conics"], d["colors"], d["opacities"], d["background"],
-                              **self.rkw)
-        rec("t3")
-        loss, v_img = ops.l2_loss(r["img"], d["target"])
-        rec("t4")
-        rb = ops.rasterize_bwd(count, s["gaussian_ids_sorted"], s["tile_bins"], p["xys"],
-                               p["conics"], d["colors"], d["opacities"], d["background"],
-                               r["final_Ts"], r["final_idx"], v_img, self.zalpha, **self.rkw)
-        rec("t5")
-        pb = ops.project_bwd(d["means3d"], d["scales"], d["quats"], d["viewmat"], p["cov3d"],
-                             p["radii"], p["conics"], p["compensation"], rb["v_xy"], self.zn,
-                             rb["v_conic"], self.zn, **kw)
-        rec("t6")
-        self.count = count
-        if self.passes is None:
-            tx = (kw["img_shape"][1] + kw["block_width"] - 1) // kw["block_width"]
-            ty = (kw["img_shape"][0] + kw["block_width"] - 1) // kw["block_width"]
-            t = tx * ty
-            end_bit = 32 + t.bit_length() + 1
-            self.passes = (end_bit + 7) // 8
-        return loss, [pb["v_mean3d"], pb["v_scale"], pb["v_quat"], rb["v_colors"],
-                      rb["v_opacity"]]
+        if ev is not None:
+            self.sess.step(mark=lambda name: ev[name].record())
+        elif self.graph:
+            self.sess.replay()
+        else:
+            self.sess.step()
+        g = self.sess.grads
+        return self.sess.loss, [g["means3d"], g["scales"], g["quats"], g["colors"],
+                                g["opacities"]]
 
     def upload(self):
-        for k, v in self.host.items():
-            self.d[k].copy_(v, non_blocking=True)
+        h = self.host
+        self.sess.set_inputs(h["means3d"], h["scales"], h["quats"], h["colors"], h["opacities"],
+                             h["viewmat"], h["background"], h["target"])
 
 
 class RefStep:
@@ -229,29 +217,38 @@ class RefStep:
 
 # ---------------------------------------------------------------------------
 
-def time_device(st, steps, warmup, flush, stage_events=False):
+def time_device(st, steps, warmup, flush):
     """Per-step CUDA-event timing, L2 flushed before each step (untimed)."""
     torch = st.torch
     for _ in range(warmup):
         st.step()
     torch.cuda.synchronize()
     total = 0.0
-    stages = {}
-    names = ["t0", "t1", "t2", "t3", "t4", "t5", "t6"]
     for _ in range(steps):
         flush.fill_(1)
-        ev = {k: torch.cuda.Event(enable_timing=True) for k in names} if stage_events else None
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        st.step(ev)
+        st.step()
         b.record()
         torch.cuda.synchronize()
         total += a.elapsed_time(b)
-        if ev:
-            for (x, y), nm in zip(zip(names, names[1:]), ["project_fwd", "count+sort", "raster_fwd",
-                                                          "l2_loss", "raster_bwd", "project_bwd"]):
-                stages[nm] = stages.get(nm, 0.0) + ev[x].elapsed_time(ev[y])
-    return total, stages
+    return total
+
+
+def time_stages(st, steps, flush):
+    """The same step run eagerly with an event before each stage (per-stage
+    device time for the roofline)."""
+    torch = st.torch
+    names = st.STAGES
+    stages = {}
+    for _ in range(steps):
+        flush.fill_(1)
+        ev = {k: torch.cuda.Event(enable_timing=True) for k in names}
+        st.step(ev)
+        torch.cuda.synchronize()
+        for x, y in zip(names, names[1:]):
+            stages[x] = stages.get(x, 0.0) + ev[x].elapsed_time(ev[y])
+    return {k: v / steps for k, v in stages.items()}
 
 
 def time_e2e(st, steps, flush):
@@ -302,6 +299,23 @@ def cpu_baseline(sc):
                       " fp32 CPU restatement, OpenMP over tiles and Gaussians)"}
 
 
+def max_over_ranks(value: float, dist=None, device=None) -> float:
+    """The slowest replica's time (the whole job waits for it)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_ms_per_step(total_ms: float, steps: int, world: int) -> float:
+    """Replicas each run `steps` steps in `total_ms` (max over ranks), so the
+    job completes world * steps steps in that time."""
+    return total_ms / (steps * world)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,6 +325,7 @@ def main():
     ap.add_argument("--scene", default="hd")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-graph", action="store_true", help="eager launches instead of a CUDA graph")
     a = ap.parse_args()
     assert a.warmup >= 3, "at least 3 warm-up steps"
 
@@ -355,31 +370,25 @@ def main():
             return
         st = RefStep(sc, dev)
     else:
-        st = OursStep(sc, dev)
+        st = OursStep(sc, dev, graph=not a.no_graph)
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        total, stages = time_device(st, a.steps, a.warmup, flush, stage_events=a.impl == "ours")
+        total = time_device(st, a.steps, a.warmup, flush)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    if dist:
-        t = torch.tensor([total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
+    total = max_over_ranks(total, dist, dev)
     e2e_ms, bi, bo = time_e2e(st, max(3, a.steps // 2), flush)
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, dist, dev)
     if rank != 0:
         dist.destroy_process_group()
         return
     ms = total / a.steps
-    value = ms / world
+    value = whole_job_ms_per_step(total, a.steps, world)
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms, 4),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -394,24 +403,29 @@ def main():
         line["cpu_baseline"] = None
         line["gpu_launches"] = None
     else:
+        st.sess.check()  # no step overflowed its capacity, no device check fired
         line["gpu_launches"] = st.launches_per_step() * a.steps
+        line["cuda_graph"] = st.graph
         count = st.count
         h, w = sc.spec.img_shape
         P = h * w
-        stage_ms = {k: v / a.steps for k, v in stages.items()}
+        stage_ms = time_stages(st, max(3, a.steps // 5), flush)
         line["stages_ms"] = {k: round(v, 4) for k, v in stage_ms.items()}
         line["num_intersects"] = count
         dominant = max(stage_ms, key=stage_ms.get)
-        # algorithmic bytes per launch ("Roofline"): raster
-        # backward reads 40 B per intersection (id + xy + opacity + conic +
-        # color) and issues 9 fp32 atomics (36 B) per (tile, Gaussian) pair,
-        # and reads 24 B per pixel (final_Ts, final_idx, v_img, v_img_alpha).
+        # algorithmic bytes per launch: raster backward gathers 40 B per
+        # intersection (4 B id + the 36 B of xy, conic, opacity and color it
+        # uses), issues 9 fp32 atomics (36 B) per (tile, Gaussian) pair, and
+        # reads 24 B per pixel (final_Ts, final_idx, v_img, v_img_alpha); the
+        # forward stage adds the packing pass (36 B in + 48 B out per Gaussian).
+        n = sc.spec.num_points
         bytes_by_stage = {"raster_bwd": 76 * count + 24 * P,
-                          "raster_fwd": 40 * count + 20 * P,
-                          "count+sort": 24 * count * st.passes + 40 * count,
+                          "raster_fwd": 40 * count + 20 * P + 84 * n,
+                          "sort": 16 * n * 4 + 28 * n + 8 * count + 16 * count * st.passes,
                           "project_fwd": 100 * sc.spec.num_points,
                           "project_bwd": 140 * sc.spec.num_points,
                           "l2_loss": 36 * P}
+        stage_ms.pop("end", None)
         peak, src = _peaks()
         achieved = bytes_by_stage[dominant] / (stage_ms[dominant] * 1e-3) / 1e9
         traffic = NCU_TRAFFIC.get(dominant)

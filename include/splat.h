@@ -109,33 +109,55 @@ SPLAT_API int splat_read_counts(const splat_params *p, const int32_t *cum_tiles_
                       uint32_t *status_out, splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
-/* Sort and bin.  Replaces ops::sort_and_bin (lib/ops.cu:645-793): key
- * emission (lib/kernels/forward.cu:135-179), a stable LSD radix sort of the
- * 64-bit tile|depth keys over bits [0, 32+msb) (CUB SortPairs at
- * lib/ops.cu:728-757; here an in-house onesweep sort) and the tile bin edges
- * (lib/kernels/forward.cu:184-208).
+/* Sort and bin.  Replaces ops::sort_and_bin (lib/ops.cu:645-793): the order
+ * of a stable LSD radix sort of the 64-bit tile|depth keys of the reference's
+ * emission (lib/kernels/forward.cu:135-179) over bits [0, 32+msb) (CUB
+ * SortPairs at lib/ops.cu:728-757), and the tile bin edges
+ * (lib/kernels/forward.cu:184-208).  Produced here by an in-house onesweep
+ * radix sort of the Gaussians by depth, emission in depth order and a stable
+ * radix sort by tile id.
  *   -> gaussian_ids_sorted (I,) int32, tile_bins (T,2) int32 (empty tiles (0,0))
- *   isect_ids / gaussian_ids (optional, may be NULL): the unsorted emission
- *   isect_ids_sorted (optional, may be NULL): the sorted keys */
+ *   isect_ids / gaussian_ids (optional, both or neither): the reference's
+ *     unsorted emission (needs cum_tiles_hit)
+ *   isect_ids_sorted (optional): the sorted 64-bit keys
+ * Counts: with count_dev == NULL, num_intersects is the exact count I.  With
+ * count_dev (a device int64, e.g. splat_project_fwd's total_out) the count is
+ * read on the device, num_intersects is the capacity the buffers and the
+ * workspace were sized for, and nothing is read back to the host (the call is
+ * CUDA-graph capturable); a count above the capacity sets the device status
+ * bit "capacity-exceeded" and leaves the outputs unusable. */
 SPLAT_API size_t splat_sort_workspace_size(const splat_params *p, int64_t num_intersects);
-SPLAT_API int splat_sort_and_bin(const splat_params *p, int64_t num_intersects, const float *xys,
-                       const float *depths, const int32_t *radii, const int32_t *cum_tiles_hit,
-                       int32_t *gaussian_ids_sorted, int32_t *tile_bins, int64_t *isect_ids,
-                       int32_t *gaussian_ids, int64_t *isect_ids_sorted, void *workspace,
-                       size_t workspace_bytes, splat_stream_t stream);
+SPLAT_API int splat_sort_and_bin(const splat_params *p, int64_t num_intersects,
+                                 const int64_t *count_dev, const float *xys,
+                                 const float *depths, const int32_t *radii,
+                                 const int32_t *cum_tiles_hit, int32_t *gaussian_ids_sorted,
+                                 int32_t *tile_bins, int64_t *isect_ids, int32_t *gaussian_ids,
+                                 int64_t *isect_ids_sorted, void *workspace,
+                                 size_t workspace_bytes, splat_stream_t stream);
 
-/* ---------------------------------------------------------------------- */
+/* Pack the rasterizer's per-Gaussian inputs into one record each: (N,12)
+ * floats, 16-byte aligned (x, y, conic a, b | conic c, opacity, r, g |
+ * b, hx, hy, 0), where (hx, hy) bound the pixels at which the Gaussian can
+ * pass the reference's alpha >= 1/255 test (a conservative box used only to
+ * skip work that test would reject).  Inputs are the reference's rasterize
+ * operands (jaxsplat/_rasterize/abstract.py:7-24):
+ *   xys (N,2) conics (N,3) colors (N,3) opacities (N,1) -> packed (N,12) */
+SPLAT_API int splat_pack_splats(const splat_params *p, const float *xys, const float *conics,
+                                const float *colors, const float *opacities, float *packed,
+                                splat_stream_t stream);
+
 /* Rasterize forward over a sorted list.  Replaces the rasterize_fwd launch of
  * ops::rasterize::fwd::xla (lib/ops.cu:144-160, kernel
  * lib/kernels/forward.cu:339-462), including the empty-list path
  * (lib/ops.cu:119-127: image = background, final_Ts = final_idx = 0).
- *   colors (N,3) opacities (N,1) background (3,) xys (N,2) conics (N,3)
+ * num_intersects / count_dev as for splat_sort_and_bin.
+ *   packed (N,12) from splat_pack_splats, background (3,)
  *   -> final_Ts (H,W,1) final_idx (H,W,1) int32 out_img (H,W,3) */
 SPLAT_API int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects,
-                        const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
-                        const float *xys, const float *conics, const float *colors,
-                        const float *opacities, const float *background, float *final_Ts,
-                        int32_t *final_idx, float *out_img, splat_stream_t stream);
+                                  const int64_t *count_dev,
+                                  const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                                  const float *packed, const float *background, float *final_Ts,
+                                  int32_t *final_idx, float *out_img, splat_stream_t stream);
 
 /* Rasterize backward over the same sorted list (no re-sort).  Replaces the
  * rasterize_bwd launch of ops::rasterize::bwd::xla (lib/ops.cu:203-225,
@@ -145,12 +167,13 @@ SPLAT_API int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects,
  *      v_xy_abs (N,2) optional: NULL skips the sum of |v_xy| that the
  *      reference computes and jaxsplat discards. */
 SPLAT_API int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
-                        const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
-                        const float *xys, const float *conics, const float *colors,
-                        const float *opacities, const float *background, const float *final_Ts,
-                        const int32_t *final_idx, const float *v_img, const float *v_img_alpha,
-                        float *v_colors, float *v_opacity, float *v_xy, float *v_xy_abs,
-                        float *v_conic, splat_stream_t stream);
+                                  const int64_t *count_dev,
+                                  const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                                  const float *packed, const float *background,
+                                  const float *final_Ts, const int32_t *final_idx,
+                                  const float *v_img, const float *v_img_alpha, float *v_colors,
+                                  float *v_opacity, float *v_xy, float *v_xy_abs, float *v_conic,
+                                  splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Projection backward.  Replaces ops::project::bwd::xla (lib/ops.cu:63-105,

@@ -130,7 +130,7 @@ def read_counts(num_points, cum_tiles_hit, total=None, device=None):
 
 
 def sort_and_bin(num_intersects, xys, depths, radii, cum_tiles_hit, *, img_shape, block_width,
-                 intermediates=False):
+                 intermediates=False, count_dev=None):
     """lib/ops.cu:645-793 -> dict(gaussian_ids_sorted, tile_bins[, isect_ids,
     gaussian_ids, isect_ids_sorted])."""
     lib = _lib.load()
@@ -148,7 +148,8 @@ def sort_and_bin(num_intersects, xys, depths, radii, cum_tiles_hit, *, img_shape
         out["isect_ids_sorted"] = torch.empty(num_intersects, dtype=torch.int64, device=dev)
     ws = _workspace(lib.splat_sort_workspace_size(C.byref(p), num_intersects), dev)
     args = [_contig(t) for t in (xys, depths, radii, cum_tiles_hit)]
-    rc = lib.splat_sort_and_bin(C.byref(p), num_intersects, *[_ptr(t) for t in args],
+    rc = lib.splat_sort_and_bin(C.byref(p), num_intersects, _ptr(count_dev),
+                                *[_ptr(t) for t in args],
                                 _ptr(out["gaussian_ids_sorted"]), _ptr(out["tile_bins"]),
                                 _ptr(out.get("isect_ids")), _ptr(out.get("gaussian_ids")),
                                 _ptr(out.get("isect_ids_sorted")), _ptr(ws), ws.numel(),
@@ -157,43 +158,57 @@ def sort_and_bin(num_intersects, xys, depths, radii, cum_tiles_hit, *, img_shape
     return out
 
 
-def rasterize_fwd(num_intersects, ids_sorted, tile_bins, xys, conics, colors, opacities,
-                  background, *, img_shape, block_width):
-    """lib/ops.cu:144-160 over a sorted list -> dict(final_Ts, final_idx, img)."""
+def pack_splats(xys, conics, colors, opacities, *, img_shape, block_width):
+    """(N, 12) packed rasterizer records (include/splat.h splat_pack_splats)."""
     lib = _lib.load()
     n = colors.shape[0]
     dev = colors.device
+    p = _params(n, img_shape, block_width=block_width, device=dev)
+    packed = torch.empty(n, 12, dtype=torch.float32, device=dev)
+    args = [_contig(t) for t in (xys, conics, colors, opacities)]
+    rc = lib.splat_pack_splats(C.byref(p), *[_ptr(t) for t in args], _ptr(packed), _stream())
+    _lib.check(rc, "pack_splats")
+    return packed
+
+
+def rasterize_fwd(num_intersects, ids_sorted, tile_bins, packed, background, *, img_shape,
+                  block_width, count_dev=None):
+    """lib/ops.cu:144-160 over a sorted list -> dict(final_Ts, final_idx, img)."""
+    lib = _lib.load()
+    n = packed.shape[0]
+    dev = packed.device
     p = _params(n, img_shape, block_width=block_width, device=dev)
     h, w = img_shape
     out = dict(final_Ts=torch.empty(h, w, 1, dtype=torch.float32, device=dev),
                final_idx=torch.empty(h, w, 1, dtype=torch.int32, device=dev),
                img=torch.empty(h, w, 3, dtype=torch.float32, device=dev))
-    args = [_contig(t) for t in (ids_sorted, tile_bins, xys, conics, colors, opacities,
-                                  background)]
-    rc = lib.splat_rasterize_fwd(C.byref(p), num_intersects, *[_ptr(t) for t in args],
+    args = [_contig(t) for t in (ids_sorted, tile_bins, packed, background)]
+    rc = lib.splat_rasterize_fwd(C.byref(p), num_intersects, _ptr(count_dev),
+                                 *[_ptr(t) for t in args],
                                  _ptr(out["final_Ts"]), _ptr(out["final_idx"]), _ptr(out["img"]),
                                  _stream())
     _lib.check(rc, "rasterize_fwd")
     return out
 
 
-def rasterize_bwd(num_intersects, ids_sorted, tile_bins, xys, conics, colors, opacities,
-                  background, final_Ts, final_idx, v_img, v_img_alpha, *, img_shape,
-                  block_width, with_abs=False):
+def rasterize_bwd(num_intersects, ids_sorted, tile_bins, packed, background, final_Ts,
+                  final_idx, v_img, v_img_alpha, *, img_shape, block_width, with_abs=False,
+                  count_dev=None):
     """lib/ops.cu:203-225 over the stored sorted list -> dict(v_colors,
     v_opacity, v_xy, v_conic[, v_xy_abs])."""
     lib = _lib.load()
-    n = colors.shape[0]
-    dev = colors.device
+    n = packed.shape[0]
+    dev = packed.device
     p = _params(n, img_shape, block_width=block_width, device=dev)
     f32 = dict(dtype=torch.float32, device=dev)
     out = dict(v_colors=torch.empty(n, 3, **f32), v_opacity=torch.empty(n, 1, **f32),
                v_xy=torch.empty(n, 2, **f32), v_conic=torch.empty(n, 3, **f32))
     if with_abs:
         out["v_xy_abs"] = torch.empty(n, 2, **f32)
-    args = [_contig(t) for t in (ids_sorted, tile_bins, xys, conics, colors, opacities,
-                                  background, final_Ts, final_idx, v_img, v_img_alpha)]
-    rc = lib.splat_rasterize_bwd(C.byref(p), num_intersects, *[_ptr(t) for t in args],
+    args = [_contig(t) for t in (ids_sorted, tile_bins, packed, background, final_Ts, final_idx,
+                                  v_img, v_img_alpha)]
+    rc = lib.splat_rasterize_bwd(C.byref(p), num_intersects, _ptr(count_dev),
+                                 *[_ptr(t) for t in args],
                                  _ptr(out["v_colors"]), _ptr(out["v_opacity"]), _ptr(out["v_xy"]),
                                  _ptr(out.get("v_xy_abs")), _ptr(out["v_conic"]), _stream())
     _lib.check(rc, "rasterize_bwd")
@@ -245,8 +260,8 @@ class ProjectFn(torch.autograd.Function):
 
 class RasterizeFn(torch.autograd.Function):
     """custom_vjp of jaxsplat/_rasterize/__init__.py:71-190.  The sorted
-    intersection list is kept as a residual, so the backward does not
-    re-emit and re-sort (lib/ops.cu:188-198 does)."""
+    intersection list and the packed records are kept as residuals, so the
+    backward does not re-emit and re-sort (lib/ops.cu:188-198 does)."""
 
     @staticmethod
     def forward(ctx, colors, opacities, background, xys, depths, radii, conics, cum_tiles_hit,
@@ -254,26 +269,27 @@ class RasterizeFn(torch.autograd.Function):
         n = colors.shape[0]
         count = read_counts(n, cum_tiles_hit, total, device=colors.device)
         s = sort_and_bin(count, xys, depths, radii, cum_tiles_hit, **kw)
-        r = rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], xys, conics, colors,
-                          opacities, background, **kw)
+        packed = pack_splats(xys, conics, colors, opacities, **kw)
+        r = rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed, background,
+                          **kw)
         ctx.kw = kw
         ctx.count = count
-        ctx.save_for_backward(colors, opacities, background, xys, conics, r["final_Ts"],
-                              r["final_idx"], s["gaussian_ids_sorted"], s["tile_bins"])
+        ctx.save_for_backward(packed, background, r["final_Ts"], r["final_idx"],
+                              s["gaussian_ids_sorted"], s["tile_bins"])
         ctx.mark_non_differentiable(r["final_idx"])
         img_alpha = 1.0 - r["final_Ts"]  # jaxsplat/_rasterize/__init__.py:136
         return r["img"], img_alpha, r["final_idx"]
 
     @staticmethod
     def backward(ctx, v_img, v_img_alpha, _fi):
-        colors, opacities, background, xys, conics, final_Ts, final_idx, ids, bins = ctx.saved_tensors
+        packed, background, final_Ts, final_idx, ids, bins = ctx.saved_tensors
         h, w = ctx.kw["img_shape"]
         if v_img is None:
-            v_img = torch.zeros(h, w, 3, dtype=torch.float32, device=colors.device)
+            v_img = torch.zeros(h, w, 3, dtype=torch.float32, device=packed.device)
         if v_img_alpha is None:  # render() drops the alpha image: zero cotangent
-            v_img_alpha = torch.zeros(h, w, 1, dtype=torch.float32, device=colors.device)
-        g = rasterize_bwd(ctx.count, ids, bins, xys, conics, colors, opacities, background,
-                          final_Ts, final_idx, v_img, v_img_alpha, **ctx.kw)
+            v_img_alpha = torch.zeros(h, w, 1, dtype=torch.float32, device=packed.device)
+        g = rasterize_bwd(ctx.count, ids, bins, packed, background, final_Ts, final_idx, v_img,
+                          v_img_alpha, **ctx.kw)
         # jaxsplat/_rasterize/__init__.py:187
         return (g["v_colors"], g["v_opacity"], None, g["v_xy"], None, None, g["v_conic"], None,
                 None, None)

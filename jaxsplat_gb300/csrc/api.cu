@@ -17,16 +17,17 @@ int launch_project_bwd(const splat_params &, const float *, const float *, const
                        const float *, const float *, const float *, const float *,
                        const float *, float *, float *, float *, float *, float *, cudaStream_t);
 size_t sort_workspace_bytes(const splat_params &, long long);
-int launch_sort_and_bin(const splat_params &, long long, const float *, const float *,
+int launch_sort_and_bin(const splat_params &, Count, const float *, const float *,
                         const int32_t *, const int32_t *, int32_t *, int2 *, long long *,
                         int32_t *, long long *, void *, size_t, cudaStream_t);
-int launch_raster_fwd(const splat_params &, long long, const int32_t *, const int2 *,
-                      const float *, const float *, const float *, const float *,
-                      const float *, float *, int32_t *, float *, cudaStream_t);
-int launch_raster_bwd(const splat_params &, long long, const int32_t *, const int2 *,
-                      const float *, const float *, const float *, const float *,
-                      const float *, const float *, const int32_t *, const float *,
-                      const float *, float *, float *, float *, float *, float *, cudaStream_t);
+int launch_pack(const splat_params &, const float *, const float *, const float *, const float *,
+                float *, cudaStream_t);
+int launch_raster_fwd(const splat_params &, Count, const int32_t *, const int2 *,
+                      const float *, const float *, float *, int32_t *, float *, cudaStream_t);
+int launch_raster_bwd(const splat_params &, Count, const int32_t *, const int2 *,
+                      const float *, const float *, const float *, const int32_t *,
+                      const float *, const float *, float *, float *, float *, float *, float *,
+                      cudaStream_t);
 
 static thread_local std::string g_error;
 
@@ -194,6 +195,7 @@ const char *splat_device_status_string(uint32_t bits) {
     if (bits & DEV_SCAN_OVERFLOW) s += "scan-overflow ";
     if (bits & DEV_BAD_TILE) s += "bad-tile ";
     if (bits & DEV_BAD_ID) s += "bad-gaussian-id ";
+    if (bits & DEV_CAPACITY) s += "capacity-exceeded ";
     if (s.empty()) s = "none";
     return s.c_str();
 }
@@ -267,47 +269,59 @@ size_t splat_sort_workspace_size(const splat_params *p, int64_t num_intersects) 
     return sort_workspace_bytes(*p, num_intersects);
 }
 
-int splat_sort_and_bin(const splat_params *p, int64_t num_intersects, const float *xys,
-                       const float *depths, const int32_t *radii, const int32_t *cum_tiles_hit,
-                       int32_t *gaussian_ids_sorted, int32_t *tile_bins, int64_t *isect_ids,
-                       int32_t *gaussian_ids, int64_t *isect_ids_sorted, void *workspace,
-                       size_t workspace_bytes, splat_stream_t stream) {
+int splat_sort_and_bin(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
+                       const float *xys, const float *depths, const int32_t *radii,
+                       const int32_t *cum_tiles_hit, int32_t *gaussian_ids_sorted,
+                       int32_t *tile_bins, int64_t *isect_ids, int32_t *gaussian_ids,
+                       int64_t *isect_ids_sorted, void *workspace, size_t workspace_bytes,
+                       splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     if (int rc = check_count(num_intersects)) return rc;
     NEED(tile_bins);
     if (num_intersects > 0) {
-        NEED(xys); NEED(depths); NEED(radii); NEED(cum_tiles_hit); NEED(gaussian_ids_sorted);
-        NEED(workspace);
+        NEED(xys); NEED(depths); NEED(radii); NEED(gaussian_ids_sorted); NEED(workspace);
+        if (isect_ids) NEED(cum_tiles_hit);
     }
-    return launch_sort_and_bin(*p, num_intersects, xys, depths, radii, cum_tiles_hit,
-                               gaussian_ids_sorted, reinterpret_cast<int2 *>(tile_bins),
+    const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
+    return launch_sort_and_bin(*p, c, xys, depths, radii, cum_tiles_hit, gaussian_ids_sorted,
+                               reinterpret_cast<int2 *>(tile_bins),
                                reinterpret_cast<long long *>(isect_ids), gaussian_ids,
                                reinterpret_cast<long long *>(isect_ids_sorted), workspace,
                                workspace_bytes, (cudaStream_t)stream);
 }
 
-int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects,
+int splat_pack_splats(const splat_params *p, const float *xys, const float *conics,
+                      const float *colors, const float *opacities, float *packed,
+                      splat_stream_t stream) {
+    if (int rc = validate(p)) return rc;
+    if (p->num_points == 0) return SPLAT_OK;
+    NEED(xys); NEED(conics); NEED(colors); NEED(opacities); NEED(packed);
+    if (reinterpret_cast<uintptr_t>(packed) % 16 || reinterpret_cast<uintptr_t>(xys) % 8)
+        return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte and xys 8-byte aligned");
+    return launch_pack(*p, xys, conics, colors, opacities, packed, (cudaStream_t)stream);
+}
+
+int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
                         const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
-                        const float *xys, const float *conics, const float *colors,
-                        const float *opacities, const float *background, float *final_Ts,
+                        const float *packed, const float *background, float *final_Ts,
                         int32_t *final_idx, float *out_img, splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     if (int rc = check_count(num_intersects)) return rc;
     NEED(background); NEED(final_Ts); NEED(final_idx); NEED(out_img);
     if (num_intersects > 0) {
-        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(xys); NEED(conics); NEED(colors);
-        NEED(opacities);
+        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed);
+        if (reinterpret_cast<uintptr_t>(packed) % 16)
+            return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
     }
-    return launch_raster_fwd(*p, num_intersects, gaussian_ids_sorted,
-                             reinterpret_cast<const int2 *>(tile_bins), xys, conics, colors,
-                             opacities, background, final_Ts, final_idx, out_img,
-                             (cudaStream_t)stream);
+    const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
+    return launch_raster_fwd(*p, c, gaussian_ids_sorted,
+                             reinterpret_cast<const int2 *>(tile_bins), packed, background,
+                             final_Ts, final_idx, out_img, (cudaStream_t)stream);
 }
 
-int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
+int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
                         const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
-                        const float *xys, const float *conics, const float *colors,
-                        const float *opacities, const float *background, const float *final_Ts,
+                        const float *packed, const float *background, const float *final_Ts,
                         const int32_t *final_idx, const float *v_img, const float *v_img_alpha,
                         float *v_colors, float *v_opacity, float *v_xy, float *v_xy_abs,
                         float *v_conic, splat_stream_t stream) {
@@ -317,14 +331,16 @@ int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
         NEED(v_colors); NEED(v_opacity); NEED(v_xy); NEED(v_conic);
     }
     if (num_intersects > 0) {
-        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(xys); NEED(conics); NEED(colors);
-        NEED(opacities); NEED(background); NEED(final_Ts); NEED(final_idx); NEED(v_img);
-        NEED(v_img_alpha);
+        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed); NEED(background);
+        NEED(final_Ts); NEED(final_idx); NEED(v_img); NEED(v_img_alpha);
+        if (reinterpret_cast<uintptr_t>(packed) % 16)
+            return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
     }
-    return launch_raster_bwd(*p, num_intersects, gaussian_ids_sorted,
-                             reinterpret_cast<const int2 *>(tile_bins), xys, conics, colors,
-                             opacities, background, final_Ts, final_idx, v_img, v_img_alpha,
-                             v_colors, v_opacity, v_xy, v_xy_abs, v_conic, (cudaStream_t)stream);
+    const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
+    return launch_raster_bwd(*p, c, gaussian_ids_sorted,
+                             reinterpret_cast<const int2 *>(tile_bins), packed, background,
+                             final_Ts, final_idx, v_img, v_img_alpha, v_colors, v_opacity, v_xy,
+                             v_xy_abs, v_conic, (cudaStream_t)stream);
 }
 
 int splat_project_bwd(const splat_params *p, const float *means3d, const float *scales,
@@ -435,6 +451,7 @@ struct SortedList {
     long long count = 0;
     int32_t *ids = nullptr;
     int32_t *bins = nullptr;
+    float *packed = nullptr;
     void *ws = nullptr;
 };
 
@@ -445,9 +462,14 @@ static int xla_sorted(const splat_params &p, void **b, cudaStream_t s, SortedLis
     const size_t ws_bytes = sort_workspace_bytes(p, L.count);
     if (cudaMallocAsync((void **)&L.bins, sizeof(int32_t) * 2 * ntiles, s) != cudaSuccess ||
         cudaMallocAsync((void **)&L.ids, sizeof(int32_t) * (size_t)(L.count ? L.count : 1), s) != cudaSuccess ||
+        cudaMallocAsync((void **)&L.packed, sizeof(float) * 12 * (size_t)(p.num_points ? p.num_points : 1), s) != cudaSuccess ||
         cudaMallocAsync(&L.ws, ws_bytes, s) != cudaSuccess)
         return check_launch("sort buffer allocation");
-    return splat_sort_and_bin(&p, L.count, (const float *)b[3], (const float *)b[4],
+    // colors b[0], opacities b[1], xys b[3], conics b[6]
+    if (int rc = splat_pack_splats(&p, (const float *)b[3], (const float *)b[6], (const float *)b[0],
+                                   (const float *)b[1], L.packed, (splat_stream_t)s))
+        return rc;
+    return splat_sort_and_bin(&p, L.count, nullptr, (const float *)b[3], (const float *)b[4],
                               (const int32_t *)b[5], cum, L.ids, L.bins, nullptr, nullptr,
                               nullptr, L.ws, ws_bytes, (splat_stream_t)s);
 }
@@ -455,6 +477,7 @@ static int xla_sorted(const splat_params &p, void **b, cudaStream_t s, SortedLis
 static void xla_release(SortedList &L, cudaStream_t s) {
     if (L.ids) cudaFreeAsync(L.ids, s);
     if (L.bins) cudaFreeAsync(L.bins, s);
+    if (L.packed) cudaFreeAsync(L.packed, s);
     if (L.ws) cudaFreeAsync(L.ws, s);
 }
 
@@ -466,10 +489,8 @@ void splat_xla_rasterize_fwd(splat_stream_t stream, void **b, const char *opaque
         SortedList L;
         rc = xla_sorted(p, b, s, L);
         if (rc == SPLAT_OK)
-            rc = splat_rasterize_fwd(&p, L.count, L.ids, L.bins, (const float *)b[3],
-                                     (const float *)b[6], (const float *)b[0],
-                                     (const float *)b[1], (const float *)b[2], (float *)b[8],
-                                     (int32_t *)b[9], (float *)b[10], stream);
+            rc = splat_rasterize_fwd(&p, L.count, nullptr, L.ids, L.bins, L.packed, (const float *)b[2],
+                                     (float *)b[8], (int32_t *)b[9], (float *)b[10], stream);
         xla_release(L, s);
     }
     report("rasterize_fwd", rc);
@@ -483,9 +504,7 @@ void splat_xla_rasterize_bwd(splat_stream_t stream, void **b, const char *opaque
         SortedList L;
         rc = xla_sorted(p, b, s, L);
         if (rc == SPLAT_OK)
-            rc = splat_rasterize_bwd(&p, L.count, L.ids, L.bins, (const float *)b[3],
-                                     (const float *)b[6], (const float *)b[0],
-                                     (const float *)b[1], (const float *)b[2],
+            rc = splat_rasterize_bwd(&p, L.count, nullptr, L.ids, L.bins, L.packed, (const float *)b[2],
                                      (const float *)b[8], (const int32_t *)b[9],
                                      (const float *)b[10], (const float *)b[11], (float *)b[12],
                                      (float *)b[13], (float *)b[14], (float *)b[15],

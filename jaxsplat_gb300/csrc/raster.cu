@@ -1,54 +1,229 @@
-// raster.cu -- tile rasterizer, forward and backward.
+// raster.cu -- tile rasterizer, forward and backward, and the per-Gaussian
+// packing pass that feeds them.
 //
-// One block per tile, one thread per pixel (block = bw x bw, bw <= 16).
+// One block per tile, one thread per pixel (bw x bw threads, bw <= 16).
 // Per-pixel arithmetic is the reference's (forward.cu:339-462,
 // backward.cu:153-343), evaluated in the same order so that final_idx and the
 // image are bit-identical; what differs is how the work is organised:
-//   forward  - batches are staged as packed float4 records (x, y, opacity,
-//              color.r) and (conic a, b, c, id) so that a batch entry is two
-//              shared-memory vector loads; colors are staged too.
-//   backward - the block starts at the largest final_idx of its pixels
-//              instead of the end of the tile list; per-Gaussian partial sums
-//              are reduced across the warp with a transposed butterfly (9
-//              shuffles for 8 values instead of 40), accumulated across the
-//              block's warps in shared memory and flushed with one global
-//              atomic per (tile, Gaussian, field) instead of one per warp.
+//
+//  * pack_kernel turns (xys, conics, colors, opacities) into one 48-byte
+//    record per Gaussian, with a conservative box around the pixels where its
+//    alpha can reach 1/255 (see below).  A staged batch entry is three
+//    16-byte loads instead of five scattered ones.
+//  * While staging a batch, each thread tests its Gaussian's box against the
+//    pixel rectangle of every warp of the tile and stores a warp mask; each
+//    warp then compacts the batch into the list of entries with its bit set
+//    and walks only those.  The skipped ones are Gaussians that the
+//    reference's per-pixel test (alpha < 1/255) rejects at every pixel of
+//    the warp anyway.
+//    For 16x16 tiles each warp covers an 8x4 pixel block (not two rows), which
+//    makes the rectangles compact and the masks sparse.
+//  * backward: the block starts at the largest final_idx of its pixels;
+//    per-Gaussian sums are reduced across the warp with a transposed butterfly
+//    (9 shuffles for 8 values) when many lanes contribute, or added per lane
+//    straight into shared memory when few do; the block's warps accumulate in
+//    shared memory and one global atomic per (tile, Gaussian, field) flushes
+//    them, instead of one per warp.
+#include <math_constants.h>
+
 #include "splat_internal.cuh"
 #include "splat_math.cuh"
 
 namespace splat {
 
 constexpr int kMaxTile = 256;  // bw * bw <= 256
+constexpr int kMaxWarps = kMaxTile / 32;
+
+// ---------------------------------------------------------------------------
+// Packing.
+//
+// Record (3 x float4):  r0 = (x, y, conic a, conic b)
+//                       r1 = (conic c, opacity, red, green)
+//                       r2 = (blue, hx, hy, 0)
+// Outside the box |px - x| <= hx, |py - y| <= hy no pixel centre passes the
+// test alpha >= 1/255 in the rasterizers' fp32 arithmetic.  hx = +inf means
+// "no bound proven" (never culled); hx = -inf means "no pixel anywhere".
+//
+// Why the box is safe: for a positive-definite conic A the exact exponent is
+// sigma = d^T A d / 2, and alpha >= 1/255 needs sigma <= thr = ln(255 o).
+// The ellipse d^T A d <= q has half-extents sqrt(q (A^-1)_xx), sqrt(q (A^-1)_yy)
+// with (A^-1)_xx = c / det, (A^-1)_yy = a / det.  The fp32 exponent differs
+// from the exact one by at most 12 kappa 2^-24 of it, kappa = the condition
+// number <= tr^2 / det; boxes are only built when tr^2 / det <= 1e4, so that
+// is below 1% and q = 2 (thr + 0.01) / 0.98 covers it, the 0.01 absorbing the
+// error of __expf and of the product o * exp.  det is formed with Kahan's
+// error-free 2x2 determinant (within 2 ulp however much a c and b^2 cancel);
+// logf and sqrtf are within 1 ulp; the half-extents get a further 0.1% and
+// 0.01 px, and Gaussians centred more than 1e5 px away are never culled, so
+// fp32 rounding of x +- hx cannot shrink the box.
+
+constexpr float kCullMargin = 0.01f;
+constexpr float kCullSigmaFactor = 0.98f;
+constexpr float kCullMaxCond = 1e4f;
+constexpr float kCullFarPx = 1e5f;
+
+struct PackArgs {
+    int n;
+    const float *xys, *conics, *colors, *opac;
+    float4 *rec;
+};
+
+__global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const float2 xy = *reinterpret_cast<const float2 *>(a.xys + 2 * (size_t)i);
+    const float ca = a.conics[3 * (size_t)i], cb = a.conics[3 * (size_t)i + 1],
+                cc = a.conics[3 * (size_t)i + 2];
+    const float o = a.opac[i];
+    const float cr = a.colors[3 * (size_t)i], cg = a.colors[3 * (size_t)i + 1],
+                cbl = a.colors[3 * (size_t)i + 2];
+    float hx = CUDART_INF_F, hy = CUDART_INF_F;
+    // det = a c - b^2 (Kahan): w = b*b rounded, e = its rounding error
+    const float w = cb * cb;
+    const float e = fmaf(cb, cb, -w);
+    const float det = fmaf(ca, cc, -w) - e;
+    const float trc = ca + cc;
+    const bool finite = isfinite(xy.x) && isfinite(xy.y) && fabsf(xy.x) < kCullFarPx &&
+                        fabsf(xy.y) < kCullFarPx && isfinite(o) && isfinite(ca) &&
+                        isfinite(cb) && isfinite(cc) && isfinite(det);
+    if (finite && ca > 0.f && cc > 0.f && det > 0.f && trc * trc <= kCullMaxCond * det && o > 0.f) {
+        const float q = 2.f * (logf(255.f * o) + kCullMargin) / kCullSigmaFactor;
+        if (q <= 0.f) {
+            hx = hy = -CUDART_INF_F;
+        } else {
+            const float ex = sqrtf(q * cc / det) * 1.001f + 0.01f;
+            const float ey = sqrtf(q * ca / det) * 1.001f + 0.01f;
+            if (ex < kCullFarPx && ey < kCullFarPx) {
+                hx = ex;
+                hy = ey;
+            }
+        }
+    }
+    float4 *r = a.rec + 3 * (size_t)i;
+    r[0] = make_float4(xy.x, xy.y, ca, cb);
+    r[1] = make_float4(cc, o, cr, cg);
+    r[2] = make_float4(cbl, hx, hy, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Pixel layout and warp rectangles.
+
+// Thread -> pixel of the tile.  16x16 tiles: warp w covers the 8x4 block at
+// ((w & 1) * 8, (w >> 1) * 4); other widths: row-major.
+template <bool k8x4>
+__device__ __forceinline__ void pixel_of(int tr, int bw, int &tx, int &ty) {
+    if (k8x4) {
+        const int w = tr >> 5, l = tr & 31;
+        tx = ((w & 1) << 3) | (l & 7);
+        ty = ((w >> 1) << 2) | (l >> 3);
+    } else {
+        tx = tr % bw;
+        ty = tr / bw;
+    }
+}
+
+// Bounding rectangle of the pixel centres of warp w, in image coordinates
+// (x_lo, x_hi, y_lo, y_hi).
+template <bool k8x4>
+__device__ __forceinline__ float4 warp_rect(int w, int bw, int bsize, float ox, float oy) {
+    int x0, x1, y0, y1;
+    if (k8x4) {
+        x0 = (w & 1) * 8;
+        x1 = x0 + 7;
+        y0 = (w >> 1) * 4;
+        y1 = y0 + 3;
+    } else {
+        const int first = 32 * w, last = min(first + 31, bsize - 1);
+        y0 = first / bw;
+        y1 = last / bw;
+        if (y0 == y1) {
+            x0 = first % bw;
+            x1 = last % bw;
+        } else {
+            x0 = 0;
+            x1 = bw - 1;
+        }
+    }
+    return make_float4(ox + (float)x0 + 0.5f, ox + (float)x1 + 0.5f, oy + (float)y0 + 0.5f,
+                       oy + (float)y1 + 0.5f);
+}
+
+// Bit w set unless Gaussian (x, y, hx, hy) provably misses warp w.  NaN
+// anywhere keeps the bit.
+__device__ __forceinline__ unsigned warp_mask(float x, float y, float hx, float hy,
+                                              const float4 *rects, int nwarps) {
+    unsigned m = 0;
+#pragma unroll
+    for (int w = 0; w < kMaxWarps; ++w) {
+        if (w >= nwarps) break;
+        const float4 r = rects[w];
+        const bool out = (x + hx < r.x) || (x - hx > r.y) || (y + hy < r.z) || (y - hy > r.w);
+        if (!out) m |= 1u << w;
+    }
+    return m;
+}
+
+// Compacts, in order, the batch entries t in [t0, n) whose mask has this
+// warp's bit into list[]; returns their number.  Warp-synchronous over the
+// lanes in wmask.
+__device__ __forceinline__ int warp_list(const unsigned *mask, int t0, int n, int warp, int lane,
+                                         unsigned wmask, uint8_t *list) {
+    int cnt = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    const int lanes = __popc(wmask);  // a partial last warp has lanes 0 .. lanes-1
+    for (int base = t0; base < n; base += lanes) {
+        const int t = base + lane;
+        const bool keep = t < n && ((mask[t] >> warp) & 1u);
+        const unsigned bal = __ballot_sync(wmask, keep);
+        if (keep) list[cnt + __popc(bal & lt)] = (uint8_t)t;
+        cnt += __popc(bal);
+    }
+    __syncwarp(wmask);
+    return cnt;
+}
+
+// ---------------------------------------------------------------------------
+// Forward.
 
 struct RasterFwdArgs {
     unsigned tiles_x, width, height, bw;
     int n;
     uint32_t *status;
-    long long count;
+    Count count;
     const int32_t *ids;
     const int2 *bins;
-    const float *xys, *conics, *colors, *opac, *background;
+    const float4 *rec;
+    const float *background;
     float *final_Ts;
     int32_t *final_idx;
     float *img;
 };
 
+template <bool k8x4>
 __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
-    __shared__ float4 s_xyoc[kMaxTile];  // x, y, opacity, red
-    __shared__ float4 s_con[kMaxTile];   // conic a, b, c, green
+    __shared__ float4 s_r0[kMaxTile];
+    __shared__ float4 s_r1[kMaxTile];
     __shared__ float s_blue[kMaxTile];
+    __shared__ unsigned s_mask[kMaxTile];
+    __shared__ float4 s_rect[kMaxWarps];
+    __shared__ uint8_t s_list[kMaxWarps][kMaxTile];
     const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
-    const unsigned i = blockIdx.y * a.bw + threadIdx.y;
-    const unsigned j = blockIdx.x * a.bw + threadIdx.x;
-    const int tr = threadIdx.y * a.bw + threadIdx.x;
+    const int tr = threadIdx.x;
     const int bsize = a.bw * a.bw;
+    const int lane = tr & 31, warp = tr >> 5, nwarps = (bsize + 31) >> 5;
+    const unsigned wmask = (warp == nwarps - 1 && (bsize & 31)) ? ((1u << (bsize & 31)) - 1u)
+                                                                : 0xffffffffu;
+    int tx, ty;
+    pixel_of<k8x4>(tr, a.bw, tx, ty);
+    const unsigned i = blockIdx.y * a.bw + ty;
+    const unsigned j = blockIdx.x * a.bw + tx;
     const float px = (float)j + 0.5f;
     const float py = (float)i + 0.5f;
     const bool inside = i < a.height && j < a.width;
     const size_t pix = (size_t)i * a.width + j;
     const float3 bg = make_float3(a.background[0], a.background[1], a.background[2]);
 
-    if (a.count == 0) {  // lib/ops.cu:119-127: background image, zero T and index
+    if (a.count.get() == 0) {  // lib/ops.cu:119-127: background image, zero T and index
         if (inside) {
             a.final_Ts[pix] = 0.f;
             a.final_idx[pix] = 0;
@@ -58,39 +233,42 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
         }
         return;
     }
+    if (tr < nwarps)
+        s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)(blockIdx.x * a.bw),
+                                     (float)(blockIdx.y * a.bw));
     const int2 range = a.bins[tile];
     bool done = !inside;
     float T = 1.f;
     int cur_idx = 0;
     float3 acc = make_float3(0.f, 0.f, 0.f);
     for (int start = range.x; start < range.y; start += bsize) {
-        if (__syncthreads_count(done) >= bsize) break;
+        if (__syncthreads_count(done) >= bsize) break;  // also publishes s_rect
         const int idx = start + tr;
         if (idx < range.y) {
             const int g = a.ids[idx];
             if (g >= 0 && g < a.n) {
-                const float2 xy = *reinterpret_cast<const float2 *>(a.xys + 2 * (size_t)g);
-                const float o = a.opac[g];
-                const float *c = a.colors + 3 * (size_t)g;
-                const float *k = a.conics + 3 * (size_t)g;
-                s_xyoc[tr] = make_float4(xy.x, xy.y, o, c[0]);
-                s_con[tr] = make_float4(k[0], k[1], k[2], c[1]);
-                s_blue[tr] = c[2];
-            } else {  // corrupt list entry: a zero-opacity record never contributes
+                const float4 r0 = a.rec[3 * (size_t)g];
+                const float4 r1 = a.rec[3 * (size_t)g + 1];
+                const float4 r2 = a.rec[3 * (size_t)g + 2];
+                s_r0[tr] = r0;
+                s_r1[tr] = r1;
+                s_blue[tr] = r2.x;
+                s_mask[tr] = warp_mask(r0.x, r0.y, r2.y, r2.z, s_rect, nwarps);
+            } else {  // corrupt list entry: never contributes
                 raise_status(a.status, DEV_BAD_ID);
-                s_xyoc[tr] = make_float4(0.f, 0.f, 0.f, 0.f);
-                s_con[tr] = make_float4(0.f, 0.f, 0.f, 0.f);
-                s_blue[tr] = 0.f;
+                s_mask[tr] = 0u;
             }
         }
         __syncthreads();
         const int n = min(bsize, range.y - start);
-        for (int t = 0; t < n && !done; ++t) {
-            const float4 xo = s_xyoc[t];
-            const float4 cc = s_con[t];
-            const float dx = xo.x - px, dy = xo.y - py;
-            const float sigma = falloff(cc.x, cc.y, cc.z, dx, dy);
-            const float alpha = fminf(0.999f, xo.z * __expf(-sigma));
+        const int cnt = warp_list(s_mask, 0, n, warp, lane, wmask, s_list[warp]);
+        for (int k = 0; k < cnt && !done; ++k) {
+            const int t = s_list[warp][k];
+            const float4 r0 = s_r0[t];
+            const float4 r1 = s_r1[t];
+            const float dx = r0.x - px, dy = r0.y - py;
+            const float sigma = falloff(r0.z, r0.w, r1.x, dx, dy);
+            const float alpha = fminf(0.999f, r1.y * __expf(-sigma));
             if (sigma < 0.f || alpha < 1.f / 255.f) continue;
             const float next_T = T * (1.f - alpha);
             if (next_T <= 1e-4f) {
@@ -98,8 +276,8 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
                 break;
             }
             const float vis = alpha * T;
-            acc.x = acc.x + xo.w * vis;
-            acc.y = acc.y + cc.w * vis;
+            acc.x = acc.x + r1.z * vis;
+            acc.y = acc.y + r1.w * vis;
             acc.z = acc.z + s_blue[t] * vis;
             T = next_T;
             cur_idx = start + t;
@@ -119,7 +297,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
 
 // Sum of 8 values over the warp, transposed: on return lane L holds the
 // warp total of value (L >> 2) & 7.  `lane` is the caller's lane index (the
-// blocks here are two-dimensional, so threadIdx.x is not the lane).
+// pixel layout decides it, not threadIdx.x).
 __device__ __forceinline__ float warp_sum8_transposed(const float v[8], int lane) {
     float b[4], c[2];
     const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
@@ -152,36 +330,46 @@ __device__ __forceinline__ float warp_sum(float v) {
 // Gradient fields accumulated per staged Gaussian.
 enum { G_R, G_G, G_B, G_CA, G_CB, G_CC, G_X, G_Y, G_OP, G_AX, G_AY, G_FIELDS };
 
+// With at most this many contributing lanes a warp adds per lane into shared
+// memory instead of reducing across the warp first.
+constexpr int kFewLanes = 4;
+
 struct RasterBwdArgs {
     unsigned tiles_x, width, height, bw;
     int n;
     uint32_t *status;
-    long long count;
+    Count count;
     const int32_t *ids;
     const int2 *bins;
-    const float *xys, *conics, *colors, *opac, *background;
+    const float4 *rec;
+    const float *background;
     const float *final_Ts;
     const int32_t *final_idx;
     const float *v_img, *v_alpha;
     float *v_colors, *v_opac, *v_xy, *v_xy_abs, *v_conic;
 };
 
-template <bool kAbs>
+template <bool k8x4, bool kAbs>
 __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
-    __shared__ float4 s_xyo[kMaxTile];  // x, y, opacity, -
-    __shared__ float4 s_con[kMaxTile];  // conic a, b, c, -
-    __shared__ float4 s_rgb[kMaxTile];  // r, g, b, -
+    __shared__ float4 s_r0[kMaxTile];
+    __shared__ float4 s_r1[kMaxTile];
+    __shared__ float s_blue[kMaxTile];
+    __shared__ unsigned s_mask[kMaxTile];
     __shared__ int s_gid[kMaxTile];
     __shared__ float s_acc[kMaxTile][G_FIELDS];
     __shared__ int s_touched[kMaxTile];
-    __shared__ int s_wmax[kMaxTile / 32];
+    __shared__ int s_wmax[kMaxWarps];
+    __shared__ float4 s_rect[kMaxWarps];
+    __shared__ uint8_t s_list[kMaxWarps][kMaxTile];
 
     const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
-    const unsigned i = blockIdx.y * a.bw + threadIdx.y;
-    const unsigned j = blockIdx.x * a.bw + threadIdx.x;
-    const int tr = threadIdx.y * a.bw + threadIdx.x;
+    const int tr = threadIdx.x;
     const int bsize = a.bw * a.bw;
     const int lane = tr & 31, warp = tr >> 5, nwarps = (bsize + 31) >> 5;
+    int tx, ty;
+    pixel_of<k8x4>(tr, a.bw, tx, ty);
+    const unsigned i = blockIdx.y * a.bw + ty;
+    const unsigned j = blockIdx.x * a.bw + tx;
     const float px = (float)j + 0.5f;
     const float py = (float)i + 0.5f;
     const bool inside = i < a.height && j < a.width;
@@ -190,6 +378,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
     const size_t pix = min((size_t)i * a.width + j, npix - 1);
     const float3 bg = make_float3(a.background[0], a.background[1], a.background[2]);
 
+    if (a.count.get() == 0) return;  // lib/ops.cu:184-186: gradients stay zero
     const float T_final = a.final_Ts[pix];
     float T = T_final;
     float3 buf = make_float3(0.f, 0.f, 0.f);
@@ -198,12 +387,14 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
     const float v_out_alpha = a.v_alpha[pix];
     const int2 range = a.bins[tile];
 
-    // partial warps (bw not a multiple of the warp size) vote with a full mask
-    // over the lanes that exist
+    // a partial last warp (bw*bw not a multiple of 32) votes over its lanes only
     const unsigned wmask = (warp == nwarps - 1 && (bsize & 31)) ? ((1u << (bsize & 31)) - 1u)
                                                                 : 0xffffffffu;
     const int warp_bin_final = __reduce_max_sync(wmask, bin_final);
     if (lane == 0) s_wmax[warp] = warp_bin_final;
+    if (tr < nwarps)
+        s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)(blockIdx.x * a.bw),
+                                     (float)(blockIdx.y * a.bw));
     __syncthreads();
     int block_max = 0;
     for (int w = 0; w < nwarps; ++w) block_max = max(block_max, s_wmax[w]);
@@ -216,19 +407,18 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
         if (idx >= range.x) {
             const int g = a.ids[idx];
             if (g >= 0 && g < a.n) {
+                const float4 r0 = a.rec[3 * (size_t)g];
+                const float4 r1 = a.rec[3 * (size_t)g + 1];
+                const float4 r2 = a.rec[3 * (size_t)g + 2];
                 s_gid[tr] = g;
-                const float2 xy = *reinterpret_cast<const float2 *>(a.xys + 2 * (size_t)g);
-                s_xyo[tr] = make_float4(xy.x, xy.y, a.opac[g], 0.f);
-                const float *k = a.conics + 3 * (size_t)g;
-                s_con[tr] = make_float4(k[0], k[1], k[2], 0.f);
-                const float *c = a.colors + 3 * (size_t)g;
-                s_rgb[tr] = make_float4(c[0], c[1], c[2], 0.f);
-            } else {  // corrupt list entry: zero opacity, never valid, never flushed
+                s_r0[tr] = r0;
+                s_r1[tr] = r1;
+                s_blue[tr] = r2.x;
+                s_mask[tr] = warp_mask(r0.x, r0.y, r2.y, r2.z, s_rect, nwarps);
+            } else {  // corrupt list entry: never contributes, never flushed
                 raise_status(a.status, DEV_BAD_ID);
                 s_gid[tr] = 0;
-                s_xyo[tr] = make_float4(0.f, 0.f, 0.f, 0.f);
-                s_con[tr] = make_float4(0.f, 0.f, 0.f, 0.f);
-                s_rgb[tr] = make_float4(0.f, 0.f, 0.f, 0.f);
+                s_mask[tr] = 0u;
             }
         }
 #pragma unroll
@@ -236,22 +426,26 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
         s_touched[tr] = 0;
         __syncthreads();
         const int n = min(bsize, batch_end + 1 - range.x);
-        for (int t = max(0, batch_end - warp_bin_final); t < n; ++t) {
+        const int cnt = warp_list(s_mask, max(0, batch_end - warp_bin_final), n, warp, lane, wmask,
+                                  s_list[warp]);
+        for (int k = 0; k < cnt; ++k) {
+            const int t = s_list[warp][k];
             bool valid = inside && (batch_end - t <= bin_final);
             float alpha = 0.f, opac = 0.f, vis = 0.f;
             float2 delta = make_float2(0.f, 0.f);
-            float4 con = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
             if (valid) {
-                con = s_con[t];
-                const float4 xo = s_xyo[t];
-                opac = xo.z;
-                delta = make_float2(xo.x - px, xo.y - py);
-                const float sigma = falloff(con.x, con.y, con.z, delta.x, delta.y);
+                r0 = s_r0[t];
+                r1 = s_r1[t];
+                opac = r1.y;
+                delta = make_float2(r0.x - px, r0.y - py);
+                const float sigma = falloff(r0.z, r0.w, r1.x, delta.x, delta.y);
                 vis = __expf(-sigma);
                 alpha = fminf(0.99f, opac * vis);
                 if (sigma < 0.f || alpha < 1.f / 255.f) valid = false;
             }
-            if (!__any_sync(wmask, valid)) continue;
+            const unsigned vmask = __ballot_sync(wmask, valid);
+            if (!vmask) continue;
             float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             float g_op = 0.f, g_ax = 0.f, g_ay = 0.f;
             if (valid) {
@@ -262,37 +456,35 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                 g8[G_R] = fac * v_out.x;
                 g8[G_G] = fac * v_out.y;
                 g8[G_B] = fac * v_out.z;
-                const float4 rgb = s_rgb[t];
-                v_a += (rgb.x * T - buf.x * ra) * v_out.x;
-                v_a += (rgb.y * T - buf.y * ra) * v_out.y;
-                v_a += (rgb.z * T - buf.z * ra) * v_out.z;
+                const float cr = r1.z, cg = r1.w, cb = s_blue[t];
+                v_a += (cr * T - buf.x * ra) * v_out.x;
+                v_a += (cg * T - buf.y * ra) * v_out.y;
+                v_a += (cb * T - buf.z * ra) * v_out.z;
                 v_a += T_final * ra * v_out_alpha;
                 v_a += -T_final * ra * bg.x * v_out.x;
                 v_a += -T_final * ra * bg.y * v_out.y;
                 v_a += -T_final * ra * bg.z * v_out.z;
-                buf.x += rgb.x * fac;
-                buf.y += rgb.y * fac;
-                buf.z += rgb.z * fac;
+                buf.x += cr * fac;
+                buf.y += cg * fac;
+                buf.z += cb * fac;
                 const float v_sigma = -opac * vis * v_a;
                 g8[G_CA] = 0.5f * v_sigma * delta.x * delta.x;
                 g8[G_CB] = v_sigma * delta.x * delta.y;
                 g8[G_CC] = 0.5f * v_sigma * delta.y * delta.y;
-                g8[G_X] = v_sigma * (con.x * delta.x + con.y * delta.y);
-                g8[G_Y] = v_sigma * (con.y * delta.x + con.z * delta.y);
+                g8[G_X] = v_sigma * (r0.z * delta.x + r0.w * delta.y);
+                g8[G_Y] = v_sigma * (r0.w * delta.x + r1.x * delta.y);
                 g_op = vis * v_a;
                 if (kAbs) {
                     g_ax = fabsf(g8[G_X]);
                     g_ay = fabsf(g8[G_Y]);
                 }
             }
-            if (wmask == 0xffffffffu) {
+            if (lane == __ffs(vmask) - 1) s_touched[t] = 1;
+            if (wmask == 0xffffffffu && __popc(vmask) > kFewLanes) {
                 const float s8 = warp_sum8_transposed(g8, lane);
                 const float sop = warp_sum(g_op);
                 if ((lane & 3) == 0) atomicAdd(&s_acc[t][lane >> 2], s8);
-                if (lane == 0) {
-                    atomicAdd(&s_acc[t][G_OP], sop);
-                    s_touched[t] = 1;
-                }
+                if (lane == 0) atomicAdd(&s_acc[t][G_OP], sop);
                 if (kAbs) {
                     const float sax = warp_sum(g_ax), say = warp_sum(g_ay);
                     if (lane == 0) {
@@ -301,7 +493,6 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                     }
                 }
             } else if (valid) {
-                // partial warp: plain shared atomics per lane
 #pragma unroll
                 for (int f = 0; f < 8; ++f) atomicAdd(&s_acc[t][f], g8[f]);
                 atomicAdd(&s_acc[t][G_OP], g_op);
@@ -309,7 +500,6 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                     atomicAdd(&s_acc[t][G_AX], g_ax);
                     atomicAdd(&s_acc[t][G_AY], g_ay);
                 }
-                s_touched[t] = 1;
             }
         }
         __syncthreads();
@@ -336,24 +526,37 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
 // ---------------------------------------------------------------------------
 // Host launchers.
 
-int launch_raster_fwd(const splat_params &p, long long count, const int32_t *ids,
-                      const int2 *bins, const float *xys, const float *conics,
-                      const float *colors, const float *opac, const float *background,
+int launch_pack(const splat_params &p, const float *xys, const float *conics,
+                const float *colors, const float *opac, float *rec, cudaStream_t s) {
+    PackArgs a;
+    a.n = (int)p.num_points;
+    a.xys = xys; a.conics = conics; a.colors = colors; a.opac = opac;
+    a.rec = reinterpret_cast<float4 *>(rec);
+    if (a.n == 0) return SPLAT_OK;
+    pack_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    return check_launch("pack_kernel");
+}
+
+int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,
+                      const int2 *bins, const float *rec, const float *background,
                       float *final_Ts, int32_t *final_idx, float *img, cudaStream_t s) {
     RasterFwdArgs a;
     a.tiles_x = tiles_x(p); a.width = p.img_width; a.height = p.img_height; a.bw = p.block_width;
     a.n = (int)p.num_points; a.status = p.device_status;
     a.count = count; a.ids = ids; a.bins = bins;
-    a.xys = xys; a.conics = conics; a.colors = colors; a.opac = opac; a.background = background;
+    a.rec = reinterpret_cast<const float4 *>(rec); a.background = background;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
-    dim3 grid(tiles_x(p), tiles_y(p)), block(p.block_width, p.block_width);
-    raster_fwd_kernel<<<grid, block, 0, s>>>(a);
+    dim3 grid(tiles_x(p), tiles_y(p));
+    const unsigned threads = p.block_width * p.block_width;
+    if (p.block_width == 16)
+        raster_fwd_kernel<true><<<grid, threads, 0, s>>>(a);
+    else
+        raster_fwd_kernel<false><<<grid, threads, 0, s>>>(a);
     return check_launch("raster_fwd_kernel");
 }
 
-int launch_raster_bwd(const splat_params &p, long long count, const int32_t *ids,
-                      const int2 *bins, const float *xys, const float *conics,
-                      const float *colors, const float *opac, const float *background,
+int launch_raster_bwd(const splat_params &p, Count count, const int32_t *ids,
+                      const int2 *bins, const float *rec, const float *background,
                       const float *final_Ts, const int32_t *final_idx, const float *v_img,
                       const float *v_alpha, float *v_colors, float *v_opac, float *v_xy,
                       float *v_xy_abs, float *v_conic, cudaStream_t s) {
@@ -365,20 +568,25 @@ int launch_raster_bwd(const splat_params &p, long long count, const int32_t *ids
         cudaMemsetAsync(v_conic, 0, n * 3 * sizeof(float), s) != cudaSuccess ||
         (v_xy_abs && cudaMemsetAsync(v_xy_abs, 0, n * 2 * sizeof(float), s) != cudaSuccess))
         return check_launch("raster_bwd output memset");
-    if (count == 0) return SPLAT_OK;  // lib/ops.cu:184-186
+    if (count.cap == 0) return SPLAT_OK;  // lib/ops.cu:184-186
     RasterBwdArgs a;
     a.tiles_x = tiles_x(p); a.width = p.img_width; a.height = p.img_height; a.bw = p.block_width;
     a.n = (int)p.num_points; a.status = p.device_status;
     a.count = count; a.ids = ids; a.bins = bins;
-    a.xys = xys; a.conics = conics; a.colors = colors; a.opac = opac; a.background = background;
+    a.rec = reinterpret_cast<const float4 *>(rec); a.background = background;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.v_img = v_img; a.v_alpha = v_alpha;
     a.v_colors = v_colors; a.v_opac = v_opac; a.v_xy = v_xy; a.v_xy_abs = v_xy_abs;
     a.v_conic = v_conic;
-    dim3 grid(tiles_x(p), tiles_y(p)), block(p.block_width, p.block_width);
-    if (v_xy_abs)
-        raster_bwd_kernel<true><<<grid, block, 0, s>>>(a);
-    else
-        raster_bwd_kernel<false><<<grid, block, 0, s>>>(a);
+    dim3 grid(tiles_x(p), tiles_y(p));
+    const unsigned threads = p.block_width * p.block_width;
+    const bool wide = p.block_width == 16;
+    if (v_xy_abs) {
+        if (wide) raster_bwd_kernel<true, true><<<grid, threads, 0, s>>>(a);
+        else raster_bwd_kernel<false, true><<<grid, threads, 0, s>>>(a);
+    } else {
+        if (wide) raster_bwd_kernel<true, false><<<grid, threads, 0, s>>>(a);
+        else raster_bwd_kernel<false, false><<<grid, threads, 0, s>>>(a);
+    }
     return check_launch("raster_bwd_kernel");
 }
 

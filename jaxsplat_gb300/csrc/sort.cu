@@ -1,131 +1,57 @@
-// sort.cu -- intersection key emission, stable onesweep LSD radix sort of the
-// 64-bit tile|depth keys, and tile bin edges.
+// sort.cu -- intersection ordering: depth sort of the Gaussians, tile-key
+// emission, stable tile sort, tile bin edges.
 //
 // Output contract (lib/ops.cu:645-793): gaussian_ids_sorted is the stable
-// ascending order of the keys over bits [0, end_bit), end_bit = 32 + msb with
-// msb = bitlength(T) + 1 (lib/ops.cu:723-724); ties keep emission order.
-// tile_bins[t] = [first, last+1) of tile t in that order, (0,0) when empty.
+// ascending order of the keys (tile << 32 | depth_bits) over bits
+// [0, end_bit), end_bit = 32 + bitlength(T) + 1 (lib/ops.cu:723-724), of the
+// reference's emission order (Gaussian index, then row-major tile); so within
+// a tile, entries are ordered by depth bits and ties by Gaussian index.
+// tile_bins[t] = [first, last + 1) of tile t in that order, (0, 0) when empty.
 //
-// Radix sort: one histogram pass over the keys computes the digit counts of
-// every 8-bit digit position at once; then one "onesweep" kernel per digit
-// position (Adinets & Merrill, "Onesweep: A Faster Least Significant Digit
-// Radix Sort for GPUs", 2022): each block takes a 3072-key partition by
-// ticket, ranks its keys stably with warp match/popc, publishes its per-digit
-// counts, resolves their global offsets with a decoupled look-back over the
-// preceding partitions and scatters keys+ids through shared memory, so every
-// pass reads and writes each key once.
+// How it is produced here (same order, a quarter of the memory traffic of a
+// 6-pass sort of 12-byte pairs):
+//  1. the N Gaussians are sorted by their 32-bit depth bits (stable, so equal
+//     depths stay in index order; Gaussians that hit no tile sort last);
+//  2. intersections are emitted in that depth order: (tile id, Gaussian id)
+//     pairs of 4 + 4 bytes, each block finding its output offset with a
+//     decoupled look-back over the preceding blocks' counts;
+//  3. the pairs are sorted stably by tile id alone (ceil(bitlength(T-1) / 8)
+//     passes: 2 at 1920x1080) -- stability keeps the depth order inside a
+//     tile;
+//  4. bin edges come from a binary search per tile.
+// Sorting uses an in-house onesweep LSD radix sort (Adinets & Merrill,
+// "Onesweep: A Faster Least Significant Digit Radix Sort for GPUs", 2022):
+// one histogram pass computes the digit counts of every pass; each pass is
+// one kernel in which a block takes a 4096-key partition by ticket, ranks its
+// keys stably with warp match/popc, publishes its per-digit counts, resolves
+// their global offsets by a decoupled look-back over preceding partitions and
+// scatters through shared memory.
+#include <algorithm>
+
 #include "splat_internal.cuh"
 #include "splat_math.cuh"
 
 namespace splat {
 
 // ---------------------------------------------------------------------------
-// Key emission (forward.cu:135-179).  A block owns 256 consecutive Gaussians;
-// their tile rectangles are expanded cooperatively so that consecutive
-// threads write consecutive slots (the reference loops per thread over the
-// rectangle, which serialises large Gaussians and scatters the writes).
-
-constexpr int kEmitBlock = 256;
-
-struct EmitArgs {
-    int n;
-    const float *xys, *depths;
-    const int32_t *radii, *cum;
-    unsigned tiles_x, tiles_y, bw;
-    long long count;
-    unsigned long long *keys;
-    int32_t *ids;
-    uint32_t *status;
-};
-
-__global__ void __launch_bounds__(kEmitBlock) emit_kernel(EmitArgs a) {
-    __shared__ int s_off[kEmitBlock + 1];  // block-local exclusive offsets
-    __shared__ int s_start[kEmitBlock];    // global first slot (cum[g-1])
-    __shared__ unsigned s_x0[kEmitBlock], s_y0[kEmitBlock], s_w[kEmitBlock];
-    __shared__ int s_dbits[kEmitBlock];
-    const int t = threadIdx.x;
-    const int g = blockIdx.x * kEmitBlock + t;
-    int cnt = 0;
-    if (g < a.n) {
-        const int rad = a.radii[g];
-        if (rad > 0) {
-            const float2 c = make_float2(a.xys[2 * g], a.xys[2 * g + 1]);
-            const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
-            s_x0[t] = r.x0;
-            s_y0[t] = r.y0;
-            s_w[t] = r.x1 - r.x0;
-            cnt = (int)((r.x1 - r.x0) * (r.y1 - r.y0));
-            s_dbits[t] = __float_as_int(a.depths[g]);
-        }
-        s_start[t] = g == 0 ? 0 : a.cum[g - 1];
-    }
-    // block exclusive scan of cnt
-    const int lane = t & 31, warp = t >> 5;
-    int v = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += u;
-    }
-    __shared__ int s_warp[kEmitBlock / 32];
-    if (lane == 31) s_warp[warp] = v;
-    __syncthreads();
-    if (t == 0) {
-        int run = 0;
-        for (int w = 0; w < kEmitBlock / 32; ++w) {
-            const int x = s_warp[w];
-            s_warp[w] = run;
-            run += x;
-        }
-        s_off[kEmitBlock] = run;
-    }
-    __syncthreads();
-    s_off[t] = s_warp[warp] + v - cnt;
-    __syncthreads();
-    const int total = s_off[kEmitBlock];
-    for (int s = t; s < total; s += kEmitBlock) {
-        // owner: last j with s_off[j] <= s (skips Gaussians with no slots)
-        int lo = 0, hi = kEmitBlock - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_off[mid] <= s) lo = mid; else hi = mid - 1;
-        }
-        const int j = lo;
-        const int k = s - s_off[j];
-        const unsigned w = s_w[j];
-        const unsigned ty = s_y0[j] + (unsigned)k / w;
-        const unsigned tx = s_x0[j] + (unsigned)k % w;
-        const long long slot = (long long)s_start[j] + k;
-        if (slot < 0 || slot >= a.count) {
-            raise_status(a.status, DEV_EMIT_OVERFLOW);
-            continue;
-        }
-        const unsigned long long tile = (unsigned long long)(ty * a.tiles_x + tx);
-        const unsigned long long key = (tile << 32) | (unsigned long long)(long long)s_dbits[j];
-        a.keys[slot] = key;
-        a.ids[slot] = blockIdx.x * kEmitBlock + j;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Radix sort.
+// Onesweep radix sort of 32-bit keys with 32-bit values.
 
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
-constexpr int kMaxPasses = 8;
+constexpr int kMaxPasses = 4;
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 12;
-constexpr int kPartKeys = kSortThreads * kSortItems;  // 3072 keys per partition
+constexpr int kSortItems = 16;
+constexpr int kPartKeys = kSortThreads * kSortItems;  // 4096 keys per partition
 constexpr int kHistCopies = 4;
 
-__device__ __forceinline__ unsigned digit_of(unsigned long long key, int shift, unsigned mask) {
-    return (unsigned)(key >> shift) & mask;
+__device__ __forceinline__ unsigned digit_of(uint32_t key, int shift, unsigned mask) {
+    return (key >> shift) & mask;
 }
 
 struct HistArgs {
-    const unsigned long long *keys;
-    long long count;
+    const uint32_t *keys;
+    Count count;
     int passes;
     int end_bit;
     unsigned *hist;  // [passes][256]
@@ -138,8 +64,9 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(HistArgs a) {
     __syncthreads();
     const int copy = (threadIdx.x >> 5) & (kHistCopies - 1);
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += stride) {
-        const unsigned long long k = a.keys[i];
+    const long long count = a.count.get();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const uint32_t k = a.keys[i];
         for (int d = 0; d < a.passes; ++d) {
             const int shift = d * kRadixBits;
             const int bits = min(kRadixBits, a.end_bit - shift);
@@ -193,11 +120,11 @@ __device__ __forceinline__ void publish_word(uint32_t *slot, uint32_t w) {
 }
 
 struct PassArgs {
-    const unsigned long long *keys_in;
+    const uint32_t *keys_in;
     const int32_t *vals_in;
-    unsigned long long *keys_out;
+    uint32_t *keys_out;
     int32_t *vals_out;
-    long long count;
+    Count count;
     int shift;
     unsigned mask;
     const unsigned *offs;  // [256] exclusive global digit offsets of this pass
@@ -207,11 +134,11 @@ struct PassArgs {
     uint32_t spin_limit;
 };
 
-__global__ void __launch_bounds__(kSortThreads) onesweep_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kSortThreads, 3) onesweep_kernel(PassArgs a) {
     __shared__ unsigned s_whist[kSortWarps][kRadix];  // per-warp digit counts -> exclusive offsets
     __shared__ unsigned s_bstart[kRadix];             // block-local digit start
     __shared__ unsigned s_gbase[kRadix];              // global position of the block's first key of digit
-    __shared__ unsigned long long s_keys[kPartKeys];
+    __shared__ uint32_t s_keys[kPartKeys];
     __shared__ int32_t s_vals[kPartKeys];
     __shared__ int s_part;
 
@@ -220,29 +147,33 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(PassArgs a) {
     for (int i = lane; i < kRadix; i += 32) s_whist[warp][i] = 0u;
     __syncthreads();
     const int part = s_part;
+    const long long count = a.count.get();
+    if ((long long)part * kPartKeys >= count) return;  // past the end (capacity-sized grid)
+    // warp-striped: warp w owns keys [base, base + 32*items), item k of lane l
+    // is key base + 32k + l, so (k, l) order is key order
     const long long base = (long long)part * kPartKeys + (long long)warp * 32 * kSortItems;
 
-    unsigned long long key[kSortItems];
+    uint32_t key[kSortItems];
     int32_t val[kSortItems];
     unsigned rank[kSortItems];
-    unsigned dig[kSortItems];
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         const long long idx = base + k * 32 + lane;
-        const bool ok = idx < a.count;
-        key[k] = ok ? a.keys_in[idx] : 0ull;
+        const bool ok = idx < count;
+        key[k] = ok ? a.keys_in[idx] : 0u;
         val[k] = ok ? a.vals_in[idx] : 0;
-        dig[k] = ok ? digit_of(key[k], a.shift, a.mask) : (unsigned)kRadix;  // kRadix = absent
+        rank[k] = ok ? 0u : 0xffffffffu;  // absent marker
     }
     const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
-        const unsigned d = dig[k];
+        const bool ok = rank[k] == 0u;
+        const unsigned d = ok ? digit_of(key[k], a.shift, a.mask) : (unsigned)kRadix;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const unsigned before = s_whist[warp][d & (kRadix - 1)];
         __syncwarp();
-        rank[k] = before + __popc(peers & lt_mask);
-        if (d < (unsigned)kRadix && lane == __ffs(peers) - 1) s_whist[warp][d] = before + __popc(peers);
+        rank[k] = ok ? before + __popc(peers & lt_mask) : 0xffffffffu;
+        if (ok && lane == __ffs(peers) - 1) s_whist[warp][d] = before + __popc(peers);
         __syncwarp();
     }
     __syncthreads();
@@ -287,21 +218,23 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(PassArgs a) {
     // stage in digit order
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
-        const unsigned d = dig[k];
-        if (d < (unsigned)kRadix) {
+        if (rank[k] != 0xffffffffu) {
+            const unsigned d = digit_of(key[k], a.shift, a.mask);
             const unsigned pos = s_bstart[d] + s_whist[warp][d] + rank[k];
-            s_keys[pos] = key[k];
-            s_vals[pos] = val[k];
+            if (pos < (unsigned)kPartKeys) {
+                s_keys[pos] = key[k];
+                s_vals[pos] = val[k];
+            }
         }
     }
     __syncthreads();
-    const long long remaining = a.count - (long long)part * kPartKeys;
+    const long long remaining = count - (long long)part * kPartKeys;
     const int nvalid = remaining < kPartKeys ? (int)remaining : kPartKeys;
     for (int i = t; i < nvalid; i += kSortThreads) {
-        const unsigned long long k = s_keys[i];
+        const uint32_t k = s_keys[i];
         const unsigned d = digit_of(k, a.shift, a.mask);
         const long long g = (long long)s_gbase[d] + (i - (int)s_bstart[d]);
-        if (g < 0 || g >= a.count) {
+        if (g < 0 || g >= count) {
             raise_status(a.status, DEV_SORT_OVERFLOW);
             continue;
         }
@@ -310,159 +243,425 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(PassArgs a) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// Tile bin edges: one thread per tile, binary search of the tile field of the
-// sorted keys (masked to the sorted bits).  Writes every tile, (0,0) when
-// empty, so no zeroing pass is needed (the reference memsets then marks the
-// boundaries, forward.cu:184-208).
-
-struct BinArgs {
-    const unsigned long long *keys;
-    long long count;
-    unsigned long long mask;
-    int ntiles;
-    int2 *bins;
+struct RadixBufs {
+    uint32_t *ka, *kb;
+    int32_t *va, *vb;
+    unsigned *hist, *offs, *tickets;
+    uint32_t *lookback;
+    size_t zero_bytes;  // hist + tickets + lookback, contiguous from hist
+    long long nparts;
+    int passes;
 };
 
-__device__ __forceinline__ long long lower_tile(const BinArgs &a, unsigned long long tile) {
-    long long lo = 0, hi = a.count;
+static RadixBufs radix_layout(Arena &ar, long long count, int end_bit) {
+    RadixBufs b;
+    b.passes = (end_bit + kRadixBits - 1) / kRadixBits;
+    b.nparts = (count + kPartKeys - 1) / kPartKeys;
+    b.ka = ar.take<uint32_t>(count);
+    b.kb = ar.take<uint32_t>(count);
+    b.va = ar.take<int32_t>(count);
+    b.vb = ar.take<int32_t>(count);
+    b.offs = ar.take<unsigned>((size_t)kMaxPasses * kRadix);
+    const size_t before = (ar.used + 255) & ~size_t(255);
+    b.hist = ar.take<unsigned>((size_t)kMaxPasses * kRadix);
+    b.tickets = ar.take<unsigned>(kMaxPasses);
+    b.lookback = ar.take<uint32_t>((size_t)b.passes * b.nparts * kRadix);
+    b.zero_bytes = ar.used - before;
+    return b;
+}
+
+// Sorts (ka, va) by the low end_bit bits of the keys.  Returns the buffers
+// holding the result; the last pass writes the values to vals_final instead
+// when it is given.
+static int radix_sort(const splat_params &p, const RadixBufs &b, Count count, int end_bit,
+                      int32_t *vals_final, const uint32_t **keys_sorted,
+                      const int32_t **vals_sorted, cudaStream_t s) {
+    if (count.cap > (long long)kLbMask)
+        return fail(SPLAT_ERR_OVERFLOW, "sort of %lld keys exceeds %u", count.cap, kLbMask);
+    *keys_sorted = b.ka;
+    *vals_sorted = b.va;
+    if (count.cap == 0) return SPLAT_OK;
+    if (cudaMemsetAsync(b.hist, 0, b.zero_bytes, s) != cudaSuccess)
+        return check_launch("sort workspace memset");
+    HistArgs h{b.ka, count, b.passes, end_bit, b.hist};
+    long long blocks = (count.cap + 256 * 16 - 1) / (256 * 16);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    radix_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(h);
+    if (int rc = check_launch("radix_hist_kernel")) return rc;
+    radix_offsets_kernel<<<b.passes, kRadix, 0, s>>>(b.hist, b.offs);
+    if (int rc = check_launch("radix_offsets_kernel")) return rc;
+    uint32_t *kin = b.ka, *kout = b.kb;
+    int32_t *vin = b.va, *vout = b.vb;
+    for (int d = 0; d < b.passes; ++d) {
+        const bool last = d == b.passes - 1;
+        PassArgs pa;
+        pa.keys_in = kin;
+        pa.vals_in = vin;
+        pa.keys_out = kout;
+        pa.vals_out = (last && vals_final) ? vals_final : vout;
+        pa.count = count;
+        pa.shift = d * kRadixBits;
+        pa.mask = (1u << min(kRadixBits, end_bit - d * kRadixBits)) - 1u;
+        pa.offs = b.offs + d * kRadix;
+        pa.lookback = b.lookback + (size_t)d * b.nparts * kRadix;
+        pa.ticket = b.tickets + d;
+        pa.status = p.device_status;
+        pa.spin_limit = spin_limit(p);
+        onesweep_kernel<<<(unsigned)b.nparts, kSortThreads, 0, s>>>(pa);
+        if (int rc = check_launch("onesweep_kernel")) return rc;
+        kin = kout;
+        kout = (kin == b.ka) ? b.kb : b.ka;
+        int32_t *vw = pa.vals_out;
+        vin = vw;
+        vout = (vw == b.va) ? b.vb : b.va;
+    }
+    *keys_sorted = kin;
+    *vals_sorted = vin;
+    return SPLAT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1 input: 32-bit depth keys (Gaussians that hit no tile sort last).
+
+__global__ void depth_keys_kernel(int n, const float *depths, const int32_t *radii, uint32_t *keys,
+                                  int32_t *vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = radii[i] > 0 ? __float_as_uint(depths[i]) : 0xffffffffu;
+    vals[i] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2: emission in depth order.  A block owns 256 consecutive positions
+// of the depth order; their tile rectangles are expanded cooperatively so
+// that consecutive threads write consecutive slots.
+
+constexpr int kEmitBlock = 256;
+
+struct EmitSortedArgs {
+    int n;
+    const int32_t *order;  // Gaussian ids in depth order
+    const float *xys;
+    const int32_t *radii;
+    unsigned tiles_x, tiles_y, bw;
+    Count count;
+    uint32_t *tile_out;
+    int32_t *id_out;
+    unsigned long long *words;  // [0] ticket, [1 + b] look-back word of block b
+    uint32_t *status;
+    uint32_t spin_limit;
+};
+
+__global__ void __launch_bounds__(kEmitBlock) emit_sorted_kernel(EmitSortedArgs a) {
+    __shared__ int s_off[kEmitBlock + 1];
+    __shared__ unsigned s_x0[kEmitBlock], s_y0[kEmitBlock], s_w[kEmitBlock];
+    __shared__ int s_gid[kEmitBlock];
+    __shared__ unsigned long long s_warp[kEmitBlock / 32];
+    __shared__ unsigned long long s_base;
+    __shared__ int s_part;
+    const int t = threadIdx.x;
+    if (t == 0) s_part = (int)atomicAdd(&a.words[0], 1ull);
+    __syncthreads();
+    const int part = s_part;
+    const int k = part * kEmitBlock + t;
+    int cnt = 0;
+    if (k < a.n) {
+        const int g = a.order[k];
+        if (g >= 0 && g < a.n) {
+            const int rad = a.radii[g];
+            if (rad > 0) {
+                const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
+                const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
+                s_x0[t] = r.x0;
+                s_y0[t] = r.y0;
+                s_w[t] = r.x1 - r.x0;
+                s_gid[t] = g;
+                cnt = (int)((r.x1 - r.x0) * (r.y1 - r.y0));
+            }
+        } else {
+            raise_status(a.status, DEV_BAD_ID);
+        }
+    }
+    // block exclusive scan of cnt
+    const int lane = t & 31, warp = t >> 5;
+    int v = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) s_warp[warp] = (unsigned long long)v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = lane < kEmitBlock / 32 ? s_warp[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        if (lane < kEmitBlock / 32) s_warp[lane] = w;  // inclusive over warps
+        const unsigned long long block_total = __shfl_sync(0xffffffffu, w, kEmitBlock / 32 - 1);
+        unsigned long long *words = a.words + 1;
+        unsigned long long excl = 0;
+        if (part == 0) {
+            if (lane == 0) publish(&words[0], kFlagPrefix | (block_total & kValueMask));
+        } else {
+            if (lane == 0) publish(&words[part], kFlagAggregate | (block_total & kValueMask));
+            excl = warp_lookback(words, part, a.spin_limit, a.status);
+            if (lane == 0) publish(&words[part], kFlagPrefix | ((excl + block_total) & kValueMask));
+        }
+        if (lane == 0) {
+            s_base = excl;
+            s_off[kEmitBlock] = (int)block_total;
+        }
+    }
+    __syncthreads();
+    s_off[t] = (int)((warp ? s_warp[warp - 1] : 0ull) + (unsigned long long)(v - cnt));
+    __syncthreads();
+    const int total = s_off[kEmitBlock];
+    const long long base = (long long)s_base;
+    const long long count = a.count.get();
+    if (part == 0 && t == 0 && a.count.dev && *a.count.dev > a.count.cap)
+        raise_status(a.status, DEV_CAPACITY);
+    for (int s = t; s < total; s += kEmitBlock) {
+        // owner: last j with s_off[j] <= s (skips Gaussians with no slots)
+        int lo = 0, hi = kEmitBlock - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_off[mid] <= s) lo = mid; else hi = mid - 1;
+        }
+        const int j = lo;
+        const int kk = s - s_off[j];
+        const unsigned w = s_w[j];
+        const unsigned ty = s_y0[j] + (unsigned)kk / w;
+        const unsigned tx = s_x0[j] + (unsigned)kk % w;
+        const long long slot = base + s;
+        if (slot >= count) {
+            raise_status(a.status, DEV_EMIT_OVERFLOW);
+            continue;
+        }
+        a.tile_out[slot] = ty * a.tiles_x + tx;
+        a.id_out[slot] = s_gid[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Optional outputs with the reference's intermediate layouts: the unsorted
+// emission in Gaussian order (forward.cu:135-179) and the sorted 64-bit keys.
+
+struct EmitRefArgs {
+    int n;
+    const float *xys, *depths;
+    const int32_t *radii, *cum;
+    unsigned tiles_x, tiles_y, bw;
+    Count count;
+    unsigned long long *keys;
+    int32_t *ids;
+    uint32_t *status;
+};
+
+__global__ void __launch_bounds__(kEmitBlock) emit_ref_kernel(EmitRefArgs a) {
+    __shared__ int s_off[kEmitBlock + 1];
+    __shared__ int s_start[kEmitBlock];
+    __shared__ unsigned s_x0[kEmitBlock], s_y0[kEmitBlock], s_w[kEmitBlock];
+    __shared__ int s_dbits[kEmitBlock];
+    __shared__ int s_warp[kEmitBlock / 32];
+    const int t = threadIdx.x;
+    const int g = blockIdx.x * kEmitBlock + t;
+    int cnt = 0;
+    if (g < a.n) {
+        const int rad = a.radii[g];
+        if (rad > 0) {
+            const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
+            const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
+            s_x0[t] = r.x0;
+            s_y0[t] = r.y0;
+            s_w[t] = r.x1 - r.x0;
+            cnt = (int)((r.x1 - r.x0) * (r.y1 - r.y0));
+            s_dbits[t] = __float_as_int(a.depths[g]);
+        }
+        s_start[t] = g == 0 ? 0 : a.cum[g - 1];
+    }
+    const int lane = t & 31, warp = t >> 5;
+    int v = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) s_warp[warp] = v;
+    __syncthreads();
+    if (t == 0) {
+        int run = 0;
+        for (int w = 0; w < kEmitBlock / 32; ++w) {
+            const int x = s_warp[w];
+            s_warp[w] = run;
+            run += x;
+        }
+        s_off[kEmitBlock] = run;
+    }
+    __syncthreads();
+    s_off[t] = s_warp[warp] + v - cnt;
+    __syncthreads();
+    const int total = s_off[kEmitBlock];
+    const long long count = a.count.get();
+    for (int s = t; s < total; s += kEmitBlock) {
+        int lo = 0, hi = kEmitBlock - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_off[mid] <= s) lo = mid; else hi = mid - 1;
+        }
+        const int j = lo;
+        const int k = s - s_off[j];
+        const unsigned w = s_w[j];
+        const unsigned ty = s_y0[j] + (unsigned)k / w;
+        const unsigned tx = s_x0[j] + (unsigned)k % w;
+        const long long slot = (long long)s_start[j] + k;
+        if (slot < 0 || slot >= count) {
+            raise_status(a.status, DEV_EMIT_OVERFLOW);
+            continue;
+        }
+        const unsigned long long tile = (unsigned long long)(ty * a.tiles_x + tx);
+        a.keys[slot] = (tile << 32) | (unsigned long long)(long long)s_dbits[j];
+        a.ids[slot] = blockIdx.x * kEmitBlock + j;
+    }
+}
+
+__global__ void compose_keys_kernel(Count count, const uint32_t *tiles, const int32_t *ids,
+                                    const float *depths, int n, unsigned long long *keys) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count.get()) return;
+    const int g = ids[i];
+    const int dbits = (g >= 0 && g < n) ? __float_as_int(depths[g]) : 0;
+    keys[i] = ((unsigned long long)tiles[i] << 32) | (unsigned long long)(long long)dbits;
+}
+
+// ---------------------------------------------------------------------------
+// Tile bin edges: one thread per tile, binary search over the sorted tile ids.
+// Writes every tile, (0, 0) when empty, so no zeroing pass is needed (the
+// reference memsets then marks the boundaries, forward.cu:184-208).
+
+__device__ __forceinline__ long long lower_tile(const uint32_t *keys, long long count, uint32_t tile) {
+    long long lo = 0, hi = count;
     while (lo < hi) {
         const long long mid = (lo + hi) >> 1;
-        if (((a.keys[mid] & a.mask) >> 32) < tile) lo = mid + 1; else hi = mid;
+        if (keys[mid] < tile) lo = mid + 1; else hi = mid;
     }
     return lo;
 }
 
-__global__ void tile_bins_kernel(BinArgs a) {
+__global__ void tile_bins_kernel(const uint32_t *keys, Count cnt, int ntiles, int2 *bins) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.ntiles) return;
-    const long long lo = lower_tile(a, (unsigned long long)t);
-    const long long hi = lower_tile(a, (unsigned long long)t + 1);
-    a.bins[t] = lo < hi ? make_int2((int)lo, (int)hi) : make_int2(0, 0);
+    if (t >= ntiles) return;
+    const long long count = cnt.get();
+    const long long lo = lower_tile(keys, count, (uint32_t)t);
+    const long long hi = lower_tile(keys, count, (uint32_t)t + 1);
+    bins[t] = lo < hi ? make_int2((int)lo, (int)hi) : make_int2(0, 0);
 }
 
 // ---------------------------------------------------------------------------
 // Host side.
 
-int sort_end_bit(unsigned ntiles) {
-    int bits = 0;
-    while ((ntiles >> bits) != 0) ++bits;  // 32 - clz(T)
-    return 32 + bits + 1;
+static int bit_length(unsigned v) {
+    int b = 0;
+    while ((v >> b) != 0) ++b;
+    return b;
 }
 
 struct SortLayout {
-    unsigned long long *keys_a, *keys_b;
-    int32_t *vals_a, *vals_b;
-    unsigned *hist, *offs, *tickets;
-    uint32_t *lookback;
-    size_t zero_bytes;  // hist + tickets + lookback are contiguous from `hist`
+    RadixBufs g;                 // Gaussians by depth
+    unsigned long long *words;   // emission look-back words
+    RadixBufs s;                 // intersections by tile
 };
 
-static SortLayout sort_layout(Arena &ar, long long count, int passes) {
+static SortLayout sort_layout(Arena &ar, const splat_params &p, long long count) {
     SortLayout L;
-    const long long nparts = (count + kPartKeys - 1) / kPartKeys;
-    L.keys_a = ar.take<unsigned long long>(count);
-    L.keys_b = ar.take<unsigned long long>(count);
-    L.vals_a = ar.take<int32_t>(count);
-    L.vals_b = ar.take<int32_t>(count);
-    L.offs = ar.take<unsigned>((size_t)passes * kRadix);
-    const size_t before = (ar.used + 255) & ~size_t(255);
-    L.hist = ar.take<unsigned>((size_t)passes * kRadix);
-    L.tickets = ar.take<unsigned>(kMaxPasses);
-    L.lookback = ar.take<uint32_t>((size_t)passes * nparts * kRadix);
-    L.zero_bytes = ar.used - before;
+    const long long n = p.num_points;
+    L.g = radix_layout(ar, n, 32);
+    L.words = ar.take<unsigned long long>((size_t)((n + kEmitBlock - 1) / kEmitBlock + 1));
+    const int tile_bits = std::max(1, bit_length(n_tiles(p) - 1));
+    L.s = radix_layout(ar, count, tile_bits);
     return L;
 }
 
 size_t sort_workspace_bytes(const splat_params &p, long long count) {
-    const int passes = (sort_end_bit(n_tiles(p)) + kRadixBits - 1) / kRadixBits;
     Arena ar{nullptr, 0};
-    sort_layout(ar, count, passes);
+    sort_layout(ar, p, count);
     return ar.used + 256;
 }
 
-int launch_sort_and_bin(const splat_params &p, long long count, const float *xys,
+int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
                         const float *depths, const int32_t *radii, const int32_t *cum,
                         int32_t *ids_sorted, int2 *bins, long long *isect_out,
                         int32_t *ids_unsorted_out, long long *keys_sorted_out, void *ws,
                         size_t ws_bytes, cudaStream_t s) {
     const unsigned tx = tiles_x(p), ty = tiles_y(p), T = tx * ty;
-    const int end_bit = sort_end_bit(T);
-    const int passes = (end_bit + kRadixBits - 1) / kRadixBits;
+    const int n = (int)p.num_points;
     Arena ar{static_cast<char *>(ws), ws_bytes};
-    SortLayout L = sort_layout(ar, count, passes);
+    const SortLayout L = sort_layout(ar, p, count.cap);
     if (!ar.fits())
         return fail(SPLAT_ERR_WORKSPACE, "sort workspace too small: need %zu bytes, got %zu",
                     ar.used, ws_bytes);
-    if (count == 0) {
+    if (count.cap == 0 || n == 0) {
         if (cudaMemsetAsync(bins, 0, sizeof(int2) * T, s) != cudaSuccess)
             return check_launch("tile_bins memset");
         return SPLAT_OK;
     }
-    // emission
-    {
-        EmitArgs e;
-        e.n = (int)p.num_points;
+    // reference-layout intermediates, on request only
+    if (isect_out || ids_unsorted_out) {
+        if (!isect_out || !ids_unsorted_out)
+            return fail(SPLAT_ERR_INVALID_ARG, "isect_ids and gaussian_ids are requested together");
+        EmitRefArgs e;
+        e.n = n;
         e.xys = xys; e.depths = depths; e.radii = radii; e.cum = cum;
         e.tiles_x = tx; e.tiles_y = ty; e.bw = p.block_width;
         e.count = count;
-        e.keys = L.keys_a;
-        e.ids = L.vals_a;
+        e.keys = reinterpret_cast<unsigned long long *>(isect_out);
+        e.ids = ids_unsorted_out;
         e.status = p.device_status;
-        emit_kernel<<<(e.n + kEmitBlock - 1) / kEmitBlock, kEmitBlock, 0, s>>>(e);
-        if (int rc = check_launch("emit_kernel")) return rc;
+        emit_ref_kernel<<<(n + kEmitBlock - 1) / kEmitBlock, kEmitBlock, 0, s>>>(e);
+        if (int rc = check_launch("emit_ref_kernel")) return rc;
     }
-    if (isect_out && cudaMemcpyAsync(isect_out, L.keys_a, sizeof(long long) * count,
-                                     cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-        return check_launch("isect_ids copy");
-    if (ids_unsorted_out && cudaMemcpyAsync(ids_unsorted_out, L.vals_a, sizeof(int32_t) * count,
-                                            cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-        return check_launch("gaussian_ids copy");
-    if (cudaMemsetAsync(L.hist, 0, L.zero_bytes, s) != cudaSuccess)
-        return check_launch("sort workspace memset");
-    {
-        HistArgs h{L.keys_a, count, passes, end_bit, L.hist};
-        long long blocks = (count + 256 * 16 - 1) / (256 * 16);
-        if (blocks > 152 * 8) blocks = 152 * 8;
-        radix_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(h);
-        if (int rc = check_launch("radix_hist_kernel")) return rc;
-        radix_offsets_kernel<<<passes, kRadix, 0, s>>>(L.hist, L.offs);
-        if (int rc = check_launch("radix_offsets_kernel")) return rc;
+    // 1. Gaussians by depth
+    depth_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, depths, radii, L.g.ka, L.g.va);
+    if (int rc = check_launch("depth_keys_kernel")) return rc;
+    const uint32_t *gkeys;
+    const int32_t *order;
+    const Count all{nullptr, n, n};
+    if (int rc = radix_sort(p, L.g, all, 32, nullptr, &gkeys, &order, s)) return rc;
+    // 2. emission in depth order
+    const int eblocks = (n + kEmitBlock - 1) / kEmitBlock;
+    if (cudaMemsetAsync(L.words, 0, sizeof(unsigned long long) * (size_t)(eblocks + 1), s) != cudaSuccess)
+        return check_launch("emission workspace memset");
+    EmitSortedArgs e;
+    e.n = n;
+    e.order = order;
+    e.xys = xys;
+    e.radii = radii;
+    e.tiles_x = tx; e.tiles_y = ty; e.bw = p.block_width;
+    e.count = count;
+    e.tile_out = L.s.ka;
+    e.id_out = L.s.va;
+    e.words = L.words;
+    e.status = p.device_status;
+    e.spin_limit = spin_limit(p);
+    emit_sorted_kernel<<<eblocks, kEmitBlock, 0, s>>>(e);
+    if (int rc = check_launch("emit_sorted_kernel")) return rc;
+    // 3. stable sort by tile id
+    const int tile_bits = std::max(1, bit_length(T - 1));
+    const uint32_t *tiles_sorted;
+    const int32_t *ids_final;
+    if (int rc = radix_sort(p, L.s, count, tile_bits, ids_sorted, &tiles_sorted, &ids_final, s))
+        return rc;
+    if (keys_sorted_out) {
+        compose_keys_kernel<<<(unsigned)((count.cap + 255) / 256), 256, 0, s>>>(
+            count, tiles_sorted, ids_sorted, depths, n,
+            reinterpret_cast<unsigned long long *>(keys_sorted_out));
+        if (int rc = check_launch("compose_keys_kernel")) return rc;
     }
-    const long long nparts = (count + kPartKeys - 1) / kPartKeys;
-    unsigned long long *kin = L.keys_a, *kout = L.keys_b;
-    int32_t *vin = L.vals_a, *vout = L.vals_b;
-    for (int d = 0; d < passes; ++d) {
-        const bool last = d == passes - 1;
-        PassArgs pa;
-        pa.keys_in = kin;
-        pa.vals_in = vin;
-        pa.keys_out = kout;
-        pa.vals_out = last ? ids_sorted : vout;
-        pa.count = count;
-        pa.shift = d * kRadixBits;
-        pa.mask = (1u << min(kRadixBits, end_bit - d * kRadixBits)) - 1u;
-        pa.offs = L.offs + d * kRadix;
-        pa.lookback = L.lookback + (size_t)d * nparts * kRadix;
-        pa.ticket = L.tickets + d;
-        pa.status = p.device_status;
-        pa.spin_limit = spin_limit(p);
-        onesweep_kernel<<<(unsigned)nparts, kSortThreads, 0, s>>>(pa);
-        if (int rc = check_launch("onesweep_kernel")) return rc;
-        unsigned long long *tk = kin; kin = kout; kout = tk;
-        int32_t *tv = vin; vin = vout; vout = tv;
-    }
-    // kin now holds the sorted keys
-    if (keys_sorted_out && cudaMemcpyAsync(keys_sorted_out, kin, sizeof(long long) * count,
-                                           cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-        return check_launch("isect_ids_sorted copy");
-    BinArgs b;
-    b.keys = kin;
-    b.count = count;
-    b.mask = end_bit >= 64 ? ~0ull : ((1ull << end_bit) - 1ull);
-    b.ntiles = (int)T;
-    b.bins = bins;
-    tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(b);
+    // 4. bins
+    tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(tiles_sorted, count, (int)T, bins);
     return check_launch("tile_bins_kernel");
 }
 

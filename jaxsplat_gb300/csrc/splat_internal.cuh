@@ -20,6 +20,19 @@ enum : uint32_t {
     DEV_SCAN_OVERFLOW = 1u << 3,     // intersection total does not fit int32
     DEV_BAD_TILE = 1u << 4,          // a sorted key named a tile outside the grid
     DEV_BAD_ID = 1u << 5,            // a sorted list entry named a Gaussian outside [0, N)
+    DEV_CAPACITY = 1u << 6,          // the device-side count exceeded the buffers' capacity
+};
+
+// An intersection count known either on the host or in device memory (the
+// int64 total the projection writes), clamped to the buffers' capacity.
+struct Count {
+    const long long *dev;  // null: use `host`
+    long long host;
+    long long cap;
+    __device__ __forceinline__ long long get() const {
+        const long long v = dev ? *dev : host;
+        return v < 0 ? 0 : (v < cap ? v : cap);
+    }
 };
 
 constexpr uint32_t kDefaultSpinLimit = 1u << 22;

@@ -1,0 +1,198 @@
+"""A preallocated, synchronisation-free forward+backward of the render path.
+
+``RenderSession`` holds every buffer of one render (fixed Gaussian count,
+camera and image size) and enqueues the whole step -- project, sort and bin,
+rasterize forward, L2 loss against a target, rasterize backward, project
+backward -- without any host read-back: the intersection count stays on the
+device (written by the projection's scan, read by the sort and rasterizer
+kernels) and the intersection buffers are sized by a capacity.  The step can
+therefore be captured once as a CUDA graph and replayed.
+
+Capacity: by default one eager render measures the count and the capacity
+is set to 1.25x that (plus a little).  ``check()`` synchronises and raises if
+a step's count ever exceeded the capacity (its outputs are then unusable;
+build a new session with a larger capacity).
+
+This is the loop of the reference's fitting example
+(examples/single_image.py:26-40): ``mean((render(...) - target)**2)`` and its
+gradients with respect to means3d, scales, quats, colors and opacities.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import torch
+
+from . import _lib
+from ._ops import _status_word
+
+
+class RenderSession:
+    def __init__(self, num_points: int, *, img_shape, f, c, glob_scale: float = 1.0,
+                 clip_thresh: float = 0.01, block_size: int = 16, capacity: int | None = None,
+                 device="cuda"):
+        self.lib = _lib.load()
+        self.dev = torch.device(device)
+        if self.dev.index is None:
+            self.dev = torch.device("cuda", torch.cuda.current_device())
+        n = int(num_points)
+        h, w = int(img_shape[0]), int(img_shape[1])
+        self.n, self.h, self.w, self.bw = n, h, w, int(block_size)
+        self.status = _status_word(self.dev)
+        self.params = _lib.make_params(n, (h, w), f, c, glob_scale, clip_thresh, block_size,
+                                       self.status.data_ptr())
+        f32 = dict(dtype=torch.float32, device=self.dev)
+        i32 = dict(dtype=torch.int32, device=self.dev)
+        E = torch.empty
+        # inputs
+        self.means3d, self.scales = E(n, 3, **f32), E(n, 3, **f32)
+        self.quats, self.colors = E(n, 4, **f32), E(n, 3, **f32)
+        self.opacities, self.viewmat = E(n, 1, **f32), E(4, 4, **f32)
+        self.background, self.target = E(3, **f32), E(h, w, 3, **f32)
+        # projection
+        self.cov3d, self.xys, self.depths = E(n, 6, **f32), E(n, 2, **f32), E(n, 1, **f32)
+        self.radii, self.conics, self.comp = E(n, 1, **i32), E(n, 3, **f32), E(n, 1, **f32)
+        self.ntiles, self.cum = E(n, 1, **i32), E(n, 1, **i32)
+        self.total = torch.zeros(1, dtype=torch.int64, device=self.dev)
+        self.proj_ws = E(self.lib.splat_project_fwd_workspace_size(C.byref(self.params)),
+                         dtype=torch.uint8, device=self.dev)
+        # rasterizer
+        tiles = ((w + self.bw - 1) // self.bw) * ((h + self.bw - 1) // self.bw)
+        self.tile_bins = E(tiles, 2, **i32)
+        self.packed = E(n, 12, **f32)
+        self.final_Ts, self.final_idx = E(h, w, 1, **f32), E(h, w, 1, **i32)
+        self.img = E(h, w, 3, **f32)
+        self.loss, self.v_img = E(1, **f32), E(h, w, 3, **f32)
+        self.v_alpha = torch.zeros(h, w, 1, **f32)
+        # gradients
+        self.v_colors, self.v_opacity = E(n, 3, **f32), E(n, 1, **f32)
+        self.v_xy, self.v_conic = E(n, 2, **f32), E(n, 3, **f32)
+        self.zeros_n1 = torch.zeros(n, 1, **f32)
+        self.v_mean3d, self.v_scale, self.v_quat = E(n, 3, **f32), E(n, 3, **f32), E(n, 4, **f32)
+        self.v_cov2d, self.v_cov3d = E(n, 3, **f32), E(n, 6, **f32)
+        self.capacity = None
+        self.graph = None
+        if capacity is not None:
+            self._size(int(capacity))
+
+    # -- buffers -------------------------------------------------------------
+    def _size(self, capacity: int):
+        self.capacity = max(int(capacity), 1)
+        self.ids_sorted = torch.empty(self.capacity, dtype=torch.int32, device=self.dev)
+        nbytes = self.lib.splat_sort_workspace_size(C.byref(self.params), self.capacity)
+        self.sort_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
+        self.graph = None
+
+    def set_inputs(self, means3d, scales, quats, colors, opacities, viewmat, background, target):
+        for dst, src in ((self.means3d, means3d), (self.scales, scales), (self.quats, quats),
+                         (self.colors, colors), (self.opacities, opacities),
+                         (self.viewmat, viewmat), (self.background, background),
+                         (self.target, target)):
+            dst.copy_(torch.as_tensor(src).reshape(dst.shape), non_blocking=True)
+
+    def measure_capacity(self, headroom: float = 1.25) -> int:
+        """One projection with a host read of the count; sizes the buffers."""
+        self._project()
+        torch.cuda.synchronize(self.dev)
+        count = int(self.total.item())
+        self._size(int(math.ceil(count * headroom)) + 4096)
+        return count
+
+    # -- the step -------------------------------------------------------------
+    @staticmethod
+    def _p(t):
+        return C.c_void_p(t.data_ptr())
+
+    def _stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _check(self, rc, what):
+        _lib.check(rc, what)
+
+    def _project(self):
+        P, pr = self._p, C.byref(self.params)
+        self._check(self.lib.splat_project_fwd(
+            pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat), P(self.cov3d),
+            P(self.xys), P(self.depths), P(self.radii), P(self.conics), P(self.comp),
+            P(self.ntiles), P(self.cum), P(self.total), P(self.proj_ws), self.proj_ws.numel(),
+            self._stream()), "project_fwd")
+
+    def step(self, mark=None):
+        """Enqueue one forward+backward on the current stream (no host sync).
+        ``mark(stage)`` is called before each stage and with "end" after the
+        last (e.g. to record CUDA events)."""
+        if self.capacity is None:
+            self.measure_capacity()
+        P, pr, s, cap = self._p, C.byref(self.params), self._stream(), self.capacity
+        lib = self.lib
+        mark = mark or (lambda name: None)
+        mark("project_fwd")
+        self._project()
+        mark("sort")
+        self._check(lib.splat_sort_and_bin(
+            pr, cap, P(self.total), P(self.xys), P(self.depths), P(self.radii), P(self.cum),
+            P(self.ids_sorted), P(self.tile_bins), None, None, None, P(self.sort_ws),
+            self.sort_ws.numel(), s), "sort_and_bin")
+        mark("raster_fwd")
+        self._check(lib.splat_pack_splats(pr, P(self.xys), P(self.conics), P(self.colors),
+                                          P(self.opacities), P(self.packed), s), "pack_splats")
+        self._check(lib.splat_rasterize_fwd(
+            pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),
+            P(self.background), P(self.final_Ts), P(self.final_idx), P(self.img), s),
+            "rasterize_fwd")
+        mark("l2_loss")
+        self._check(lib.splat_l2_loss(P(self.img), P(self.target), self.img.numel(),
+                                      P(self.loss), P(self.v_img), s), "l2_loss")
+        mark("raster_bwd")
+        self._check(lib.splat_rasterize_bwd(
+            pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),
+            P(self.background), P(self.final_Ts), P(self.final_idx), P(self.v_img),
+            P(self.v_alpha), P(self.v_colors), P(self.v_opacity), P(self.v_xy), None,
+            P(self.v_conic), s), "rasterize_bwd")
+        mark("project_bwd")
+        self._check(lib.splat_project_bwd(
+            pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat), P(self.cov3d),
+            P(self.radii), P(self.conics), P(self.comp), P(self.v_xy), P(self.zeros_n1),
+            P(self.v_conic), P(self.zeros_n1), P(self.v_mean3d), P(self.v_scale),
+            P(self.v_quat), P(self.v_cov2d), P(self.v_cov3d), s), "project_bwd")
+        mark("end")
+
+    def capture(self):
+        """Capture step() as a CUDA graph (after one eager warm-up step)."""
+        if self.capacity is None:
+            self.measure_capacity()
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            self.step()
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step()
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def check(self) -> int:
+        """Synchronise; raise if any step overflowed or a device check fired.
+        Returns the last step's intersection count."""
+        torch.cuda.synchronize(self.dev)
+        bits = int(self.status.item())
+        count = int(self.total.item())
+        if bits:
+            self.status.zero_()
+            msg = self.lib.splat_device_status_string(bits).decode()
+            raise _lib.SplatError(f"device status: {msg} (count {count}, capacity "
+                                  f"{self.capacity})")
+        return count
+
+    @property
+    def grads(self):
+        return dict(means3d=self.v_mean3d, scales=self.v_scale, quats=self.v_quat,
+                    colors=self.v_colors, opacities=self.v_opacity)

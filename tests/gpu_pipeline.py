@@ -24,18 +24,18 @@ def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True) -> dict:
     count = _ops.read_counts(n, p["cum_tiles_hit"], p["total"], device=t["means3d"].device)
     s = _ops.sort_and_bin(count, p["xys"], p["depths"], p["radii"], p["cum_tiles_hit"],
                           img_shape=kw["img_shape"], block_width=bw, intermediates=True)
-    r = _ops.rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], p["xys"],
-                           p["conics"], t["colors"], t["opacities"], t["background"],
-                           img_shape=kw["img_shape"], block_width=bw)
+    packed = _ops.pack_splats(p["xys"], p["conics"], t["colors"], t["opacities"],
+                              img_shape=kw["img_shape"], block_width=bw)
+    r = _ops.rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed,
+                           t["background"], img_shape=kw["img_shape"], block_width=bw)
     out = {**p, **s, **r}
     out.pop("total")
     out["count"] = torch.tensor(count)
     if v_img is not None:
         h, w = kw["img_shape"]
         vi = torch.from_numpy(np.ascontiguousarray(v_img, np.float32)).cuda()
-        rb = _ops.rasterize_bwd(count, s["gaussian_ids_sorted"], s["tile_bins"], p["xys"],
-                                p["conics"], t["colors"], t["opacities"], t["background"],
-                                r["final_Ts"], r["final_idx"], vi,
+        rb = _ops.rasterize_bwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed,
+                                t["background"], r["final_Ts"], r["final_idx"], vi,
                                 torch.zeros(h, w, 1, device="cuda"), img_shape=kw["img_shape"],
                                 block_width=bw, with_abs=with_abs)
         z = torch.zeros(n, 1, device="cuda")

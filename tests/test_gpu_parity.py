@@ -228,9 +228,10 @@ def test_full_size_properties(scene):
     tile_of = (keys >> 32)
     starts = bins[:, 0][lens > 0]
     assert bool((tile_of[starts] == torch.nonzero(lens > 0).ravel()).all())
-    r = _ops.rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], p["xys"], p["conics"],
-                           t["colors"], t["opacities"], t["background"],
-                           img_shape=kw["img_shape"], block_width=16)
+    packed = _ops.pack_splats(p["xys"], p["conics"], t["colors"], t["opacities"],
+                              img_shape=kw["img_shape"], block_width=16)
+    r = _ops.rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed,
+                           t["background"], img_shape=kw["img_shape"], block_width=16)
     assert bool(torch.isfinite(r["img"]).all())
     assert int(r["final_idx"].min().item()) >= 0 and int(r["final_idx"].max().item()) < count
     assert float(r["final_Ts"].min().item()) >= 0.0 and float(r["final_Ts"].max().item()) <= 1.0
