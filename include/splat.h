@@ -195,6 +195,28 @@ SPLAT_API int splat_l2_loss(const float *img, const float *target, int64_t count
                   float *v_img, splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Fitting loop of examples/single_image.py:10-69 (quats normalised, colors
+ * and opacities through a sigmoid, optax.adam(lr) on the raw parameters).
+ * splat_fit_transform maps raw -> rendered parameters:
+ *   quats (N,4) = quats_raw / |quats_raw|, colors (N,3) = sigmoid(colors_raw),
+ *   opac (N,1) = sigmoid(opac_raw).
+ * splat_fit_adam increments the device step counter *step_dev, then applies
+ * the maps' chain rule to the render gradients (with respect to means,
+ * scales and the mapped quats, colors, opacities) and one Adam update
+ * (b1 0.9, b2 0.999, eps 1e-8) to the 14 raw parameters of every Gaussian;
+ * m and v are (N,14) moment buffers (means 3, scales 3, quats 4, colors 3,
+ * opacity 1), zero before the first step. */
+SPLAT_API int splat_fit_transform(int n, const float *quats_raw, const float *colors_raw,
+                                  const float *opac_raw, float *quats, float *colors,
+                                  float *opac, splat_stream_t stream);
+SPLAT_API int splat_fit_adam(int n, float lr, int *step_dev, float *means, float *scales,
+                             float *quats_raw, float *colors_raw, float *opac_raw, float *m,
+                             float *v, const float *g_means, const float *g_scales,
+                             const float *g_quats, const float *g_colors, const float *g_opac,
+                             const float *quats, const float *colors, const float *opac,
+                             splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Legacy XLA custom-call targets (drop-in for lib/ffi.cu:4-13).  Buffers in
  * the order of jaxsplat/_{project,rasterize}/lowering.py; opaque is the
  * 80-byte descriptor of splat_xla_make_descriptor (lib/ffi.cu:15-52). */

@@ -65,6 +65,8 @@ _SIGS = [
                                             C.c_float, C.c_uint32, _v, C.c_size_t]),
     ("splat_selftest_wait_timeout", C.c_int, [C.c_uint32, _v, _v]),
     ("splat_project_fwd_noalloc", C.c_int, [_P] + [_v] * 13 + [_v]),
+    ("splat_fit_transform", C.c_int, [C.c_int] + [_v] * 6 + [_v]),
+    ("splat_fit_adam", C.c_int, [C.c_int, C.c_float] + [_v] * 16 + [_v]),
 ]
 
 EXPORTED = [name for name, _, _ in _SIGS]

@@ -191,9 +191,21 @@ __device__ __forceinline__ TileRect tile_rect(float2 center, float radius, unsig
     return r;
 }
 
-// Gaussian falloff exponent at a pixel offset (forward.cu:424-426).
+// Gaussian falloff exponent at a pixel offset (forward.cu:424-426):
+// 0.5 * (a dx dx + c dy dy) + b dx dy, written with the explicit roundings
+// that the reference's expression compiles to -- the inner sum fuses its left
+// product, the outer sum fuses b dx dy onto the scaled inner sum.  (Measured:
+// this form reproduces the reference's image bit for bit at 1920x1080, the
+// other fusion orders do not.)  Spelling the roundings out keeps the result
+// independent of how the compiler would otherwise share products between
+// pixels that have the same dx or dy.
 __device__ __forceinline__ float falloff(float a, float b, float c, float dx, float dy) {
-    return 0.5f * (a * dx * dx + c * dy * dy) + b * dx * dy;
+    const float inner = __fmaf_rn(__fmul_rn(a, dx), dx, __fmul_rn(__fmul_rn(c, dy), dy));
+    return __fmaf_rn(__fmul_rn(b, dx), dy, __fmul_rn(0.5f, inner));
 }
+
+// pix_out + c * vis and acc + T * bg of forward.cu:443-459 (one fused
+// multiply-add each).
+__device__ __forceinline__ float blend(float acc, float c, float w) { return __fmaf_rn(c, w, acc); }
 
 }  // namespace splat

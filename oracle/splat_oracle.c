@@ -417,11 +417,12 @@ API void SYM(tile_bin_edges)(int64_t count, const int64_t *sorted_keys, int n_ti
 }
 
 /* Per-pixel Gaussian falloff exponent, forward.cu:424-426 with nvcc's
- * contraction: inner sum fuses its left product, the outer sum fuses the
- * 0.5 scale. */
+ * contraction: the inner sum fuses its left product, the outer sum fuses
+ * b dx dy onto the 0.5-scaled inner sum (the form that reproduces the
+ * reference kernel's image bit for bit). */
 static inline real falloff(const real *conic, real dx, real dy) {
     real inner = FMA(conic[0] * dx, dx, conic[2] * dy * dy);
-    return FMA(K(0.5), inner, conic[1] * dx * dy);
+    return FMA(conic[1] * dx, dy, K(0.5) * inner);
 }
 
 /* forward.cu:339-462 (and ops.cu:119-127 when there is no intersection). */

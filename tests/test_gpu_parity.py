@@ -116,6 +116,10 @@ def test_cuda_matches_live_reference(scene):
     ref = {k: v.cpu().numpy() for k, v in full.items()}
     out = run_cuda(inp, kw, 16, v_img=v_img.cpu().numpy())
     assert_parity(out, ref, label=scene)
+    # the per-pixel arithmetic is the reference's: image and transmittance
+    # come out bit for bit
+    np.testing.assert_array_equal(out["img"], ref["img"])
+    np.testing.assert_array_equal(out["final_Ts"], ref["final_Ts"])
 
 
 def _oracle_case(o, inp, kw, bw, v_img=None):
