@@ -143,10 +143,10 @@ class OursStep:
         bw = sc.spec.block_width
         tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
         tile_passes = (max(1, (tiles - 1).bit_length()) + 7) // 8
-        # project, depth keys, 4-pass depth sort (+hist, offsets), emission,
-        # tile sort (+hist, offsets), bins, pack, raster fwd, loss, raster bwd,
-        # project bwd
-        self.kernels_per_step = 1 + 1 + 6 + 1 + (2 + tile_passes) + 1 + 1 + 1 + 1 + 1 + 1
+        # project, depth keys, 4-pass depth sort (+hist, offsets), emission
+        # (offsets, expansion), tile sort (+hist, offsets), bins, pack, raster
+        # fwd, loss, raster bwd, project bwd
+        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 1 + 1 + 1 + 1
         self.passes = tile_passes
 
     def launches_per_step(self):

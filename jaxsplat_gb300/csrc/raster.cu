@@ -148,10 +148,12 @@ __device__ __forceinline__ float4 warp_rect(int w, int bw, int bsize, float ox, 
                        oy + (float)y1 + 0.5f);
 }
 
-// Bit w set unless Gaussian (x, y, hx, hy) provably misses warp w.  NaN
-// anywhere keeps the bit.
-__device__ __forceinline__ unsigned warp_mask(float x, float y, float hx, float hy,
-                                              const float4 *rects, int nwarps) {
+// Bit w set unless the Gaussian of record (r0, r2) provably misses every
+// pixel centre of warp w (they all lie outside its box).  NaN anywhere keeps
+// the bit.
+__device__ __forceinline__ unsigned warp_mask(float4 r0, float4 r2, const float4 *rects,
+                                              int nwarps) {
+    const float x = r0.x, y = r0.y, hx = r2.y, hy = r2.z;
     unsigned m = 0;
 #pragma unroll
     for (int w = 0; w < kMaxWarps; ++w) {
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
                 s_r0[tr] = r0;
                 s_r1[tr] = r1;
                 s_blue[tr] = r2.x;
-                s_mask[tr] = warp_mask(r0.x, r0.y, r2.y, r2.z, s_rect, nwarps);
+                s_mask[tr] = warp_mask(r0, r2, s_rect, nwarps);
             } else {  // corrupt list entry: never contributes
                 raise_status(a.status, DEV_BAD_ID);
                 s_mask[tr] = 0u;
@@ -382,10 +384,11 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
     if (a.count.get() == 0) return;  // lib/ops.cu:184-186: gradients stay zero
     const float T_final = a.final_Ts[pix];
     float T = T_final;
-    float3 buf = make_float3(0.f, 0.f, 0.f);
     const int bin_final = inside ? a.final_idx[pix] : 0;
     const float3 v_out = make_float3(a.v_img[3 * pix], a.v_img[3 * pix + 1], a.v_img[3 * pix + 2]);
-    const float v_out_alpha = a.v_alpha[pix];
+    // S . v_out and T_final (v_out_alpha - bg . v_out): see BwdPixel
+    float sv = 0.f;
+    const float kb = T_final * (a.v_alpha[pix] - (bg.x * v_out.x + bg.y * v_out.y + bg.z * v_out.z));
     const int2 range = a.bins[tile];
 
     // a partial last warp (bw*bw not a multiple of 32) votes over its lanes only
@@ -415,7 +418,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                 s_r0[tr] = r0;
                 s_r1[tr] = r1;
                 s_blue[tr] = r2.x;
-                s_mask[tr] = warp_mask(r0.x, r0.y, r2.y, r2.z, s_rect, nwarps);
+                s_mask[tr] = warp_mask(r0, r2, s_rect, nwarps);
             } else {  // corrupt list entry: never contributes, never flushed
                 raise_status(a.status, DEV_BAD_ID);
                 s_gid[tr] = 0;
@@ -453,21 +456,13 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                 const float ra = 1.f / (1.f - alpha);
                 T *= ra;
                 const float fac = alpha * T;
-                float v_a = 0.f;
                 g8[G_R] = fac * v_out.x;
                 g8[G_G] = fac * v_out.y;
                 g8[G_B] = fac * v_out.z;
                 const float cr = r1.z, cg = r1.w, cb = s_blue[t];
-                v_a += (cr * T - buf.x * ra) * v_out.x;
-                v_a += (cg * T - buf.y * ra) * v_out.y;
-                v_a += (cb * T - buf.z * ra) * v_out.z;
-                v_a += T_final * ra * v_out_alpha;
-                v_a += -T_final * ra * bg.x * v_out.x;
-                v_a += -T_final * ra * bg.y * v_out.y;
-                v_a += -T_final * ra * bg.z * v_out.z;
-                buf.x += cr * fac;
-                buf.y += cg * fac;
-                buf.z += cb * fac;
+                const float cv = cr * v_out.x + cg * v_out.y + cb * v_out.z;
+                const float v_a = T * cv + (kb - sv) * ra;
+                sv += fac * cv;
                 const float v_sigma = -opac * vis * v_a;
                 g8[G_CA] = 0.5f * v_sigma * delta.x * delta.x;
                 g8[G_CB] = v_sigma * delta.x * delta.y;
@@ -543,12 +538,17 @@ __device__ __forceinline__ float4 warp_rect16(int w, float ox, float oy) {
 }
 
 // Per-pixel state of the backward pass (backward.cu:181-211).
+// The running color sum S of backward.cu:193 enters the alpha cotangent
+// only as S . v_out, and the background and alpha-image terms only as
+// T_final (v_out_alpha - bg . v_out); both are carried as scalars:
+//   v_alpha = T (c . v_out) + (T_final (v_out_alpha - bg . v_out) - S . v_out) / (1 - alpha)
+// which is the reference's expression regrouped.
 struct BwdPixel {
     float py;
     bool inside;
     int bin_final;
-    float T_final, T, v_out_alpha;
-    float3 buf, v_out;
+    float T, sv, kb;  // transmittance, S . v_out, T_final (v_out_alpha - bg . v_out)
+    float3 v_out;
 };
 
 template <bool kAbs>
@@ -580,12 +580,13 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
         P[q].inside = i < a.height && j < a.width;
         // backward.cu:184: out-of-image threads read the last pixel
         const size_t pix = min((size_t)i * a.width + j, npix - 1);
-        P[q].T_final = a.final_Ts[pix];
-        P[q].T = P[q].T_final;
-        P[q].buf = make_float3(0.f, 0.f, 0.f);
+        const float T_final = a.final_Ts[pix];
+        P[q].T = T_final;
+        P[q].sv = 0.f;
         P[q].bin_final = P[q].inside ? a.final_idx[pix] : 0;
-        P[q].v_out = make_float3(a.v_img[3 * pix], a.v_img[3 * pix + 1], a.v_img[3 * pix + 2]);
-        P[q].v_out_alpha = a.v_alpha[pix];
+        const float3 vo = make_float3(a.v_img[3 * pix], a.v_img[3 * pix + 1], a.v_img[3 * pix + 2]);
+        P[q].v_out = vo;
+        P[q].kb = T_final * (a.v_alpha[pix] - (bg.x * vo.x + bg.y * vo.y + bg.z * vo.z));
     }
     const int2 range = a.bins[tile];
     const int warp_bin_final = __reduce_max_sync(0xffffffffu, max(P[0].bin_final, P[1].bin_final));
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
                     s_r0[e] = r0;
                     s_r1[e] = r1;
                     s_blue[e] = r2.x;
-                    s_mask[e] = warp_mask(r0.x, r0.y, r2.y, r2.z, s_rect, kT16Warps);
+                    s_mask[e] = warp_mask(r0, r2, s_rect, kT16Warps);
                 } else {  // corrupt list entry: never contributes, never flushed
                     raise_status(a.status, DEV_BAD_ID);
                     s_gid[e] = 0;
@@ -659,20 +660,12 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
                 const float ra = 1.f / (1.f - alpha[q]);
                 S.T *= ra;
                 const float fac = alpha[q] * S.T;
-                float v_a = 0.f;
                 g8[G_R] += fac * S.v_out.x;
                 g8[G_G] += fac * S.v_out.y;
                 g8[G_B] += fac * S.v_out.z;
-                v_a += (cr * S.T - S.buf.x * ra) * S.v_out.x;
-                v_a += (cg * S.T - S.buf.y * ra) * S.v_out.y;
-                v_a += (cb * S.T - S.buf.z * ra) * S.v_out.z;
-                v_a += S.T_final * ra * S.v_out_alpha;
-                v_a += -S.T_final * ra * bg.x * S.v_out.x;
-                v_a += -S.T_final * ra * bg.y * S.v_out.y;
-                v_a += -S.T_final * ra * bg.z * S.v_out.z;
-                S.buf.x += cr * fac;
-                S.buf.y += cg * fac;
-                S.buf.z += cb * fac;
+                const float cv = cr * S.v_out.x + cg * S.v_out.y + cb * S.v_out.z;
+                const float v_a = S.T * cv + (S.kb - S.sv) * ra;
+                S.sv += fac * cv;
                 const float v_sigma = -opac * vis[q] * v_a;
                 const float ddy = dy[q];
                 g8[G_CA] += 0.5f * v_sigma * dx * dx;

@@ -98,15 +98,25 @@ __global__ void __launch_bounds__(kRadix) radix_offsets_kernel(const unsigned *h
     offs[d * kRadix + t] = s[t] - x;
 }
 
-// 32-bit look-back words: [flag:2][count:30].
+// 32-bit look-back words: [flag:2][count:30].  The count travels inside the
+// word, so the words need no ordering against other memory: relaxed loads and
+// stores at device scope are enough.
 constexpr uint32_t kLbAgg = 1u << 30;
 constexpr uint32_t kLbPrefix = 2u << 30;
 constexpr uint32_t kLbMask = (1u << 30) - 1u;
+// Predecessor words read at once per look-back step.  The walk back to the
+// nearest published prefix is a chain of dependent L2 round trips; reading a
+// window of them together shortens the chain by the window's length.
+constexpr int kLbWindow = 8;
 
-__device__ __forceinline__ uint32_t wait_word(uint32_t *slot, uint32_t limit, uint32_t *status) {
-    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> a(*slot);
+__device__ __forceinline__ uint32_t load_word(const uint32_t *slot) {
+    cuda::atomic_ref<const uint32_t, cuda::thread_scope_device> a(*slot);
+    return a.load(cuda::memory_order_relaxed);
+}
+
+__device__ __forceinline__ uint32_t wait_word(const uint32_t *slot, uint32_t limit, uint32_t *status) {
     for (uint32_t i = 0; i < limit; ++i) {
-        const uint32_t w = a.load(cuda::memory_order_acquire);
+        const uint32_t w = load_word(slot);
         if (w & (kLbAgg | kLbPrefix)) return w;
         if (i > 32) __nanosleep(64);
     }
@@ -116,7 +126,35 @@ __device__ __forceinline__ uint32_t wait_word(uint32_t *slot, uint32_t limit, ui
 
 __device__ __forceinline__ void publish_word(uint32_t *slot, uint32_t w) {
     cuda::atomic_ref<uint32_t, cuda::thread_scope_device> a(*slot);
-    a.store(w, cuda::memory_order_release);
+    a.store(w, cuda::memory_order_relaxed);
+}
+
+// Exclusive prefix of one digit for partition `part` (> 0): the words of
+// partitions part-1, part-2, ... (stride `stride` words apart) are summed
+// down to and including the nearest one flagged as an inclusive prefix.
+__device__ __forceinline__ unsigned lookback_digit(const uint32_t *words, size_t stride, int part,
+                                                   uint32_t limit, uint32_t *status) {
+    unsigned excl = 0;
+    bool done = false;
+    for (int j = part - 1; !done; j -= kLbWindow) {
+        uint32_t w[kLbWindow];
+#pragma unroll
+        for (int i = 0; i < kLbWindow; ++i)
+            w[i] = j - i >= 0 ? load_word(words + (size_t)(j - i) * stride) : kLbPrefix;
+#pragma unroll
+        for (int i = 0; i < kLbWindow; ++i) {
+            if (!done) {
+                uint32_t x = w[i];
+                // j - i >= 0 here: partition 0 publishes a prefix, so the walk
+                // stops there at the latest
+                if (!(x & (kLbAgg | kLbPrefix)))
+                    x = wait_word(words + (size_t)(j - i) * stride, limit, status);
+                excl += x & kLbMask;
+                done = (x & kLbPrefix) != 0;
+            }
+        }
+    }
+    return excl;
 }
 
 struct PassArgs {
@@ -134,7 +172,7 @@ struct PassArgs {
     uint32_t spin_limit;
 };
 
-__global__ void __launch_bounds__(kSortThreads, 3) onesweep_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     __shared__ unsigned s_whist[kSortWarps][kRadix];  // per-warp digit counts -> exclusive offsets
     __shared__ unsigned s_bstart[kRadix];             // block-local digit start
     __shared__ unsigned s_gbase[kRadix];              // global position of the block's first key of digit
@@ -154,27 +192,28 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_kernel(PassArgs a) {
     const long long base = (long long)part * kPartKeys + (long long)warp * 32 * kSortItems;
 
     uint32_t key[kSortItems];
-    int32_t val[kSortItems];
     unsigned rank[kSortItems];
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         const long long idx = base + k * 32 + lane;
-        const bool ok = idx < count;
-        key[k] = ok ? a.keys_in[idx] : 0u;
-        val[k] = ok ? a.vals_in[idx] : 0;
-        rank[k] = ok ? 0u : 0xffffffffu;  // absent marker
+        key[k] = idx < count ? a.keys_in[idx] : 0u;
     }
+    // Stable rank of each key among the warp's keys with the same digit:
+    // the lanes holding a digit (match_any) are ranked by lane, and the
+    // lowest of them adds their number to the warp's digit counter.  The
+    // counter updates of successive items are shared-memory atomics issued
+    // in item order, so they need no barrier between items and overlap.
     const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
-        const bool ok = rank[k] == 0u;
+        const bool ok = base + k * 32 + lane < count;
         const unsigned d = ok ? digit_of(key[k], a.shift, a.mask) : (unsigned)kRadix;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const unsigned before = s_whist[warp][d & (kRadix - 1)];
-        __syncwarp();
+        const int leader = __ffs(peers) - 1;
+        unsigned before = 0;
+        if (ok && lane == leader) before = atomicAdd(&s_whist[warp][d], (unsigned)__popc(peers));
+        before = __shfl_sync(0xffffffffu, before, leader);
         rank[k] = ok ? before + __popc(peers & lt_mask) : 0xffffffffu;
-        if (ok && lane == __ffs(peers) - 1) s_whist[warp][d] = before + __popc(peers);
-        __syncwarp();
     }
     __syncthreads();
 
@@ -188,19 +227,7 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_kernel(PassArgs a) {
     }
     const unsigned cnt = run;
     uint32_t *my = a.lookback + (size_t)part * kRadix + t;
-    unsigned excl = 0;
-    if (part == 0) {
-        publish_word(my, kLbPrefix | (cnt & kLbMask));
-    } else {
-        publish_word(my, kLbAgg | (cnt & kLbMask));
-        for (int j = part - 1; j >= 0; --j) {
-            const uint32_t w = wait_word(a.lookback + (size_t)j * kRadix + t, a.spin_limit, a.status);
-            excl += w & kLbMask;
-            if (w & kLbPrefix) break;
-        }
-        publish_word(my, kLbPrefix | ((excl + cnt) & kLbMask));
-    }
-    s_gbase[t] = a.offs[t] + excl;
+    publish_word(my, (part == 0 ? kLbPrefix : kLbAgg) | (cnt & kLbMask));
     // block-local exclusive scan of the digit counts (for staging)
     s_bstart[t] = cnt;
     __syncthreads();
@@ -215,18 +242,28 @@ __global__ void __launch_bounds__(kSortThreads, 3) onesweep_kernel(PassArgs a) {
     s_bstart[t] = bstart;
     __syncthreads();
 
-    // stage in digit order
+    // stage in digit order; the values are loaded only now (coalesced, in
+    // key order) so that they take no registers during the ranking
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         if (rank[k] != 0xffffffffu) {
             const unsigned d = digit_of(key[k], a.shift, a.mask);
-            const unsigned pos = s_bstart[d] + s_whist[warp][d] + rank[k];
-            if (pos < (unsigned)kPartKeys) {
-                s_keys[pos] = key[k];
-                s_vals[pos] = val[k];
-            }
+            rank[k] += s_bstart[d] + s_whist[warp][d];
+            if (rank[k] < (unsigned)kPartKeys) s_keys[rank[k]] = key[k];
         }
     }
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        if (rank[k] < (unsigned)kPartKeys) s_vals[rank[k]] = a.vals_in[base + k * 32 + lane];
+    }
+    // look-back last, after the staging: the predecessors have had that long
+    // to publish their prefixes, and the keys are out of registers
+    unsigned excl = 0;
+    if (part > 0) {
+        excl = lookback_digit(a.lookback + t, kRadix, part, a.spin_limit, a.status);
+        publish_word(my, kLbPrefix | ((excl + cnt) & kLbMask));
+    }
+    s_gbase[t] = a.offs[t] + excl;
     __syncthreads();
     const long long remaining = count - (long long)part * kPartKeys;
     const int nvalid = remaining < kPartKeys ? (int)remaining : kPartKeys;
@@ -333,65 +370,67 @@ __global__ void depth_keys_kernel(int n, const float *depths, const int32_t *rad
 }
 
 // ---------------------------------------------------------------------------
-// Stage 2: emission in depth order.  A block owns 256 consecutive positions
-// of the depth order; their tile rectangles are expanded cooperatively so
-// that consecutive threads write consecutive slots.
+// Stage 2: emission in depth order, in two kernels.
+//
+// emit_offsets_kernel: each Gaussian's first slot, an exclusive scan of the
+// tile counts in depth order.  Large partitions (4096 positions per block,
+// 16 per thread) keep the look-back chain short: the decoupled look-back's
+// inclusive prefixes advance by one window of partitions per L2 round trip,
+// so its latency grows with the number of partitions.
+// emit_expand_kernel: a block owns 256 consecutive positions of the depth
+// order; their tile rectangles are expanded cooperatively so that
+// consecutive threads write consecutive slots.  No waiting on other blocks.
 
 constexpr int kEmitBlock = 256;
+constexpr int kOffItems = 16;
+constexpr int kOffPart = kEmitBlock * kOffItems;
 
-struct EmitSortedArgs {
+struct EmitOffsetsArgs {
     int n;
     const int32_t *order;  // Gaussian ids in depth order
     const float *xys;
     const int32_t *radii;
     unsigned tiles_x, tiles_y, bw;
-    Count count;
-    uint32_t *tile_out;
-    int32_t *id_out;
+    int32_t *offs;              // [n] first slot of each depth position (saturated at INT32_MAX)
     unsigned long long *words;  // [0] ticket, [1 + b] look-back word of block b
     uint32_t *status;
     uint32_t spin_limit;
 };
 
-__global__ void __launch_bounds__(kEmitBlock) emit_sorted_kernel(EmitSortedArgs a) {
-    __shared__ int s_off[kEmitBlock + 1];
-    __shared__ unsigned s_x0[kEmitBlock], s_y0[kEmitBlock], s_w[kEmitBlock];
-    __shared__ int s_gid[kEmitBlock];
+__device__ __forceinline__ int rect_count(const EmitOffsetsArgs &a, int g) {
+    if (g < 0 || g >= a.n) return 0;
+    const int rad = a.radii[g];
+    if (rad <= 0) return 0;
+    const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
+    const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
+    return (int)((r.x1 - r.x0) * (r.y1 - r.y0));
+}
+
+__global__ void __launch_bounds__(kEmitBlock) emit_offsets_kernel(EmitOffsetsArgs a) {
     __shared__ unsigned long long s_warp[kEmitBlock / 32];
     __shared__ unsigned long long s_base;
     __shared__ int s_part;
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) s_part = (int)atomicAdd(&a.words[0], 1ull);
     __syncthreads();
     const int part = s_part;
-    const int k = part * kEmitBlock + t;
-    int cnt = 0;
-    if (k < a.n) {
-        const int g = a.order[k];
-        if (g >= 0 && g < a.n) {
-            const int rad = a.radii[g];
-            if (rad > 0) {
-                const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
-                const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
-                s_x0[t] = r.x0;
-                s_y0[t] = r.y0;
-                s_w[t] = r.x1 - r.x0;
-                s_gid[t] = g;
-                cnt = (int)((r.x1 - r.x0) * (r.y1 - r.y0));
-            }
-        } else {
-            raise_status(a.status, DEV_BAD_ID);
-        }
+    const long long first = (long long)part * kOffPart + (long long)t * kOffItems;
+    int cnt[kOffItems];
+    long long run = 0;
+#pragma unroll
+    for (int k = 0; k < kOffItems; ++k) {
+        const long long pos = first + k;
+        cnt[k] = pos < a.n ? rect_count(a, a.order[pos]) : 0;
+        run += cnt[k];
     }
-    // block exclusive scan of cnt
-    const int lane = t & 31, warp = t >> 5;
-    int v = cnt;
+    // block exclusive scan of the per-thread totals
+    unsigned long long v = (unsigned long long)run;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        const unsigned long long u = __shfl_up_sync(0xffffffffu, v, o);
         if (lane >= o) v += u;
     }
-    if (lane == 31) s_warp[warp] = (unsigned long long)v;
+    if (lane == 31) s_warp[warp] = v;
     __syncthreads();
     if (warp == 0) {
         unsigned long long w = lane < kEmitBlock / 32 ? s_warp[lane] : 0ull;
@@ -411,18 +450,69 @@ __global__ void __launch_bounds__(kEmitBlock) emit_sorted_kernel(EmitSortedArgs 
             excl = warp_lookback(words, part, a.spin_limit, a.status);
             if (lane == 0) publish(&words[part], kFlagPrefix | ((excl + block_total) & kValueMask));
         }
-        if (lane == 0) {
-            s_base = excl;
-            s_off[kEmitBlock] = (int)block_total;
-        }
+        if (lane == 0) s_base = excl;
     }
     __syncthreads();
-    s_off[t] = (int)((warp ? s_warp[warp - 1] : 0ull) + (unsigned long long)(v - cnt));
+    unsigned long long o = s_base + (warp ? s_warp[warp - 1] : 0ull) + (v - (unsigned long long)run);
+#pragma unroll
+    for (int k = 0; k < kOffItems; ++k) {
+        const long long pos = first + k;
+        if (pos < a.n) a.offs[pos] = o < 0x7fffffffull ? (int32_t)o : 0x7fffffff;
+        o += (unsigned long long)cnt[k];
+    }
+}
+
+struct EmitExpandArgs {
+    int n;
+    const int32_t *order;
+    const int32_t *offs;
+    const float *xys;
+    const int32_t *radii;
+    unsigned tiles_x, tiles_y, bw;
+    Count count;
+    uint32_t *tile_out;
+    int32_t *id_out;
+    uint32_t *status;
+};
+
+__global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs a) {
+    __shared__ int s_off[kEmitBlock];
+    __shared__ unsigned s_x0[kEmitBlock], s_y0[kEmitBlock], s_w[kEmitBlock];
+    __shared__ int s_gid[kEmitBlock];
+    __shared__ int s_total;
+    const int t = threadIdx.x;
+    const int k0 = blockIdx.x * kEmitBlock;
+    const int k = k0 + t;
+    const int last = min(a.n, k0 + kEmitBlock) - 1;
+    long long base = a.offs[k0];
+    int cnt = 0;
+    if (k < a.n) {
+        const int g = a.order[k];
+        if (g >= 0 && g < a.n) {
+            const int rad = a.radii[g];
+            if (rad > 0) {
+                const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
+                const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
+                s_x0[t] = r.x0;
+                s_y0[t] = r.y0;
+                s_w[t] = r.x1 - r.x0;
+                s_gid[t] = g;
+                cnt = (int)((r.x1 - r.x0) * (r.y1 - r.y0));
+            }
+        } else {
+            raise_status(a.status, DEV_BAD_ID);
+        }
+        // offsets relative to the block's first slot; a saturated offset
+        // (past any capacity) lands past the count and is reported below
+        s_off[t] = (int)min((long long)a.offs[k] - base, 0x3fffffffll);
+        if (k == last) s_total = (int)min((long long)a.offs[k] - base + cnt, 0x3fffffffll);
+    } else {
+        s_off[t] = 0x7fffffff;  // never an owner
+    }
     __syncthreads();
-    const int total = s_off[kEmitBlock];
-    const long long base = (long long)s_base;
+    const int total = s_total;
     const long long count = a.count.get();
-    if (part == 0 && t == 0 && a.count.dev && *a.count.dev > a.count.cap)
+    if (blockIdx.x == 0 && t == 0 && a.count.dev && *a.count.dev > a.count.cap)
         raise_status(a.status, DEV_CAPACITY);
     for (int s = t; s < total; s += kEmitBlock) {
         // owner: last j with s_off[j] <= s (skips Gaussians with no slots)
@@ -572,6 +662,7 @@ static int bit_length(unsigned v) {
 struct SortLayout {
     RadixBufs g;                 // Gaussians by depth
     unsigned long long *words;   // emission look-back words
+    int32_t *offs;               // first slot of each depth position
     RadixBufs s;                 // intersections by tile
 };
 
@@ -579,7 +670,8 @@ static SortLayout sort_layout(Arena &ar, const splat_params &p, long long count)
     SortLayout L;
     const long long n = p.num_points;
     L.g = radix_layout(ar, n, 32);
-    L.words = ar.take<unsigned long long>((size_t)((n + kEmitBlock - 1) / kEmitBlock + 1));
+    L.words = ar.take<unsigned long long>((size_t)((n + kOffPart - 1) / kOffPart + 1));
+    L.offs = ar.take<int32_t>((size_t)n);
     const int tile_bits = std::max(1, bit_length(n_tiles(p) - 1));
     L.s = radix_layout(ar, count, tile_bits);
     return L;
@@ -631,23 +723,34 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
     const Count all{nullptr, n, n};
     if (int rc = radix_sort(p, L.g, all, 32, nullptr, &gkeys, &order, s)) return rc;
     // 2. emission in depth order
-    const int eblocks = (n + kEmitBlock - 1) / kEmitBlock;
-    if (cudaMemsetAsync(L.words, 0, sizeof(unsigned long long) * (size_t)(eblocks + 1), s) != cudaSuccess)
+    const int oblocks = (n + kOffPart - 1) / kOffPart;
+    if (cudaMemsetAsync(L.words, 0, sizeof(unsigned long long) * (size_t)(oblocks + 1), s) != cudaSuccess)
         return check_launch("emission workspace memset");
-    EmitSortedArgs e;
+    EmitOffsetsArgs eo;
+    eo.n = n;
+    eo.order = order;
+    eo.xys = xys;
+    eo.radii = radii;
+    eo.tiles_x = tx; eo.tiles_y = ty; eo.bw = p.block_width;
+    eo.offs = L.offs;
+    eo.words = L.words;
+    eo.status = p.device_status;
+    eo.spin_limit = spin_limit(p);
+    emit_offsets_kernel<<<oblocks, kEmitBlock, 0, s>>>(eo);
+    if (int rc = check_launch("emit_offsets_kernel")) return rc;
+    EmitExpandArgs e;
     e.n = n;
     e.order = order;
+    e.offs = L.offs;
     e.xys = xys;
     e.radii = radii;
     e.tiles_x = tx; e.tiles_y = ty; e.bw = p.block_width;
     e.count = count;
     e.tile_out = L.s.ka;
     e.id_out = L.s.va;
-    e.words = L.words;
     e.status = p.device_status;
-    e.spin_limit = spin_limit(p);
-    emit_sorted_kernel<<<eblocks, kEmitBlock, 0, s>>>(e);
-    if (int rc = check_launch("emit_sorted_kernel")) return rc;
+    emit_expand_kernel<<<(n + kEmitBlock - 1) / kEmitBlock, kEmitBlock, 0, s>>>(e);
+    if (int rc = check_launch("emit_expand_kernel")) return rc;
     // 3. stable sort by tile id
     const int tile_bits = std::max(1, bit_length(T - 1));
     const uint32_t *tiles_sorted;

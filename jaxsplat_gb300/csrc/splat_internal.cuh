@@ -41,14 +41,16 @@ __device__ __forceinline__ void raise_status(uint32_t *status, uint32_t bits) {
     if (status) atomicOr(status, bits);
 }
 
-// Look-back words: two flag bits over a 62-bit value.
+// Look-back words: two flag bits over a 62-bit value.  The value travels
+// inside the word and nothing else is read on its strength, so relaxed
+// device-scope loads and stores are enough.
 constexpr unsigned long long kFlagAggregate = 1ull << 62;
 constexpr unsigned long long kFlagPrefix = 2ull << 62;
 constexpr unsigned long long kValueMask = (1ull << 62) - 1ull;
 
 __device__ __forceinline__ void publish(unsigned long long *slot, unsigned long long word) {
     cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> a(*slot);
-    a.store(word, cuda::memory_order_release);
+    a.store(word, cuda::memory_order_relaxed);
 }
 
 // Poll `slot` until it holds a flagged word.  Gives up after `limit` polls
@@ -58,7 +60,7 @@ __device__ __forceinline__ unsigned long long wait_flagged(unsigned long long *s
                                                            uint32_t limit, uint32_t *status) {
     cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> a(*slot);
     for (uint32_t i = 0; i < limit; ++i) {
-        const unsigned long long w = a.load(cuda::memory_order_acquire);
+        const unsigned long long w = a.load(cuda::memory_order_relaxed);
         if (w & (kFlagAggregate | kFlagPrefix)) return w;
         if (i > 32) __nanosleep(64);
     }

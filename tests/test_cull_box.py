@@ -33,15 +33,20 @@ def box(x, y, a, b, c, o):
     return ex, ey
 
 
+def fma32(x, y, z):
+    """fp32 fused multiply-add (the product of two fp32 values is exact in
+    fp64)."""
+    return (np.asarray(x, np.float64) * np.asarray(y, np.float64) + np.asarray(z, np.float64)).astype(np.float32)
+
+
 def passes(x, y, a, b, c, o, px, py):
-    """fp32 alpha test of the forward kernel (exponent contracted the way nvcc
-    contracts the reference's expression, exp in fp32)."""
+    """fp32 alpha test of the forward kernel (the falloff's roundings as
+    splat_math.cuh spells them out, exp in fp32)."""
     f = np.float32
     dx = f(x) - px
     dy = f(y) - py
-    inner = np.fma(f(a) * dx, dx, (f(c) * dy) * dy) if hasattr(np, "fma") else f(a) * dx * dx + f(c) * dy * dy
-    sigma = f(0.5) * inner.astype(f) + (f(b) * dx) * dy
-    sigma = sigma.astype(f)
+    inner = fma32(f(a) * dx, dx, (f(c) * dy) * dy)
+    sigma = fma32(f(b) * dx, dy, f(0.5) * inner)
     alpha = np.minimum(f(0.999), f(o) * np.exp(-sigma).astype(f))
     return (sigma >= 0) & (alpha >= f(1.0) / f(255.0))
 
