@@ -41,10 +41,10 @@ METRIC = "fwd+bwd ms/iter, 1M Gaussians @1080p"
 UNIT = "ms"
 L2_FLUSH_BYTES = 256 << 20
 
-# DRAM bytes of one raster_bwd_kernel launch on the 1M-Gaussian 1920x1080
-# scene, from `ncu --section MemoryWorkloadAnalysis` (profiles/raster_bwd_hd.md);
-# None until captured.
-NCU_TRAFFIC = {"raster_bwd": None}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the dominant kernel on the 1M-Gaussian 1920x1080 scene, from the ncu capture
+# summarised in profiles/raster_bwd16_hd.md (104.17 MB read + 4.87 MB written).
+NCU_TRAFFIC = {"raster_bwd": 104_166_400 + 4_871_168}
 
 
 def _peaks():
@@ -152,6 +152,20 @@ class OursStep:
     def launches_per_step(self):
         return self.kernels_per_step
 
+    def stage_bytes(self):
+        """Algorithmic bytes per stage: raster backward gathers 40 B per
+        intersection (4 B id + the 36 B of xy, conic, opacity and color it
+        uses), issues 9 fp32 atomics (36 B) per (tile, Gaussian) pair, and
+        reads 24 B per pixel (final_Ts, final_idx, v_img, v_img_alpha); the
+        forward stage adds the packing pass (36 B in + 48 B out per
+        Gaussian)."""
+        n, I = self.sc.spec.num_points, self.count
+        h, w = self.sc.spec.img_shape
+        P = h * w
+        return {"raster_bwd": 76 * I + 24 * P, "raster_fwd": 40 * I + 20 * P + 84 * n,
+                "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes,
+                "project_fwd": 100 * n, "project_bwd": 140 * n, "l2_loss": 36 * P}
+
     def step(self, ev=None):
         if ev is not None:
             self.sess.step(mark=lambda name: ev[name].record())
@@ -209,6 +223,137 @@ class RefStep:
                             rb["v_xy"], self.zn, rb["v_conic"], **kw)
         return loss, [pb["v_mean3d"], pb["v_scale"], pb["v_quat"], rb["v_colors"],
                       rb["v_opacity"]]
+
+    def upload(self):
+        for k, v in self.host.items():
+            self.d[k].copy_(v, non_blocking=True)
+
+
+class BatchStep:
+    """The batched workload: 4 scenes x 8 views with mixed image sizes, all
+    views in one pass of each kernel (jaxsplat_gb300.BatchSession), one CUDA
+    graph per step."""
+
+    STAGES = OursStep.STAGES
+
+    def __init__(self, seed, dev, graph=True, autotune=False, log=None):
+        import torch
+
+        from jaxsplat_gb300.batch import BatchSession
+        from jaxsplat_gb300.scenes import make_batch
+
+        self.torch, self.dev = torch, dev
+        scenes, views, targets = make_batch(seed)
+        self.views = views
+        self.sess = BatchSession(scenes, views, targets, block_size=16, chunk=1, device=dev)
+        self.tuning = None
+        if autotune:
+            self.tuning = self.sess.autotune(log=log)
+        s = self.sess
+        cat = lambda k, w: torch.from_numpy(np.concatenate(
+            [np.reshape(x[k], (-1, w)) for x in scenes]).astype(np.float32)).pin_memory()
+        self.host = {"means3d": cat("means3d", 3), "scales": cat("scales", 3),
+                     "quats": cat("quats", 4), "colors": cat("colors", 3),
+                     "opacities": cat("opacities", 1), "target": s.target.cpu().pin_memory()}
+        self.count = s.measure_capacity()
+        self.graph = graph
+        if graph:
+            s.capture()
+        b = s.batch
+        tile_passes = (max(1, (int(b.num_tiles) - 1).bit_length()) + 7) // 8
+        # project, depth keys, 4-pass depth sort (+hist, offsets), emission
+        # (2), tile sort (+hist, offsets), bins, tile costs, 3-pass cost sort
+        # (+hist, offsets), pack, raster fwd, loss, raster bwd, project bwd
+        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 5 + 1 + 1 + 1 + 1 + 1
+        self.passes = tile_passes
+
+    def launches_per_step(self):
+        return self.kernels_per_step
+
+    def stage_bytes(self):
+        """As OursStep.stage_bytes over E (view, Gaussian) entries."""
+        b, I = self.sess.batch, self.count
+        E, P = int(b.num_entries), int(b.num_pixels)
+        return {"raster_bwd": 76 * I + 24 * P, "raster_fwd": 40 * I + 20 * P + 84 * E,
+                "sort": 16 * E * 4 + 28 * E + 8 * I + 16 * I * self.passes,
+                "project_fwd": 100 * E, "project_bwd": 140 * E, "l2_loss": 36 * P}
+
+    def step(self, ev=None):
+        if ev is not None:
+            self.sess.step(mark=lambda name: ev[name].record())
+        elif self.graph:
+            self.sess.replay()
+        else:
+            self.sess.step()
+        s = self.sess
+        return s.loss, [s.v_mean3d, s.v_scale, s.v_quat, s.v_colors, s.v_opacity]
+
+    def upload(self):
+        s, h = self.sess, self.host
+        for dst, k in ((s.means3d, "means3d"), (s.scales, "scales"), (s.quats, "quats"),
+                       (s.colors, "colors"), (s.opacities, "opacities"), (s.target, "target")):
+            dst.copy_(h[k], non_blocking=True)
+
+
+class RefBatchStep:
+    """The batched workload through the reference's kernels the way a
+    jaxsplat user runs it: one render call per view, scene gradients summed
+    over the views."""
+
+    def __init__(self, seed, dev):
+        import torch
+
+        from jaxsplat_gb300.scenes import make_batch
+        from oracle.ref import RefKernels
+
+        self.torch, self.dev = torch, dev
+        self.rk = RefKernels()
+        scenes, views, targets = make_batch(seed)
+        self.views = views
+        self.host = {}
+        for i, x in enumerate(scenes):
+            for k, v in x.items():
+                self.host[f"{i}:{k}"] = torch.from_numpy(np.ascontiguousarray(v)).pin_memory()
+        for i, t in enumerate(targets):
+            self.host[f"t{i}"] = torch.from_numpy(t).pin_memory()
+        self.d = {k: v.to(dev) for k, v in self.host.items()}
+        self.scenes = [{k: self.d[f"{i}:{k}"] for k in x} for i, x in enumerate(scenes)]
+        self.targets = [self.d[f"t{i}"] for i in range(len(targets))]
+        self.vm = [torch.from_numpy(v["viewmat"]).to(dev) for v in views]
+        self.bg = [torch.from_numpy(np.asarray(v["background"], np.float32)).to(dev) for v in views]
+
+    def launches_per_step(self):
+        return 0
+
+    def step(self, ev=None):
+        torch, rk = self.torch, self.rk
+        loss = 0.0
+        grads = [[torch.zeros_like(x[k]) for k in ("means3d", "scales", "quats", "colors",
+                                                     "opacities")] for x in self.scenes]
+        for k, v in enumerate(self.views):
+            d = self.scenes[v["scene"]]
+            h, w = v["img_shape"]
+            kw = dict(img_shape=(h, w), f=v["f"], c=v["c"], glob_scale=1.0, clip_thresh=0.01,
+                      block_width=16)
+            ikw = dict(img_shape=(h, w), block_width=16)
+            zn = torch.zeros(d["means3d"].shape[0], 1, device=self.dev)
+            p = rk.project_fwd(d["means3d"], d["scales"], d["quats"], self.vm[k], **kw)
+            r = rk.rasterize_fwd(d["colors"], d["opacities"], self.bg[k], p["xys"], p["depths"],
+                                 p["radii"], p["conics"], p["cum_tiles_hit"], **ikw)
+            img = r["img"]
+            loss = loss + ((img - self.targets[k]) ** 2).mean()
+            v_img = (2.0 * (img - self.targets[k]) / img.numel()).contiguous()
+            rb = rk.rasterize_bwd(d["colors"], d["opacities"], self.bg[k], p["xys"], p["depths"],
+                                  p["radii"], p["conics"], p["cum_tiles_hit"], r["final_Ts"],
+                                  r["final_idx"], v_img, torch.zeros(h, w, 1, device=self.dev),
+                                  **ikw)
+            pb = rk.project_bwd(d["means3d"], d["scales"], d["quats"], self.vm[k], p["cov3d"],
+                                p["xys"], p["radii"], p["conics"], p["compensation"], zn,
+                                rb["v_xy"], zn, rb["v_conic"], **kw)
+            for acc, g in zip(grads[v["scene"]], (pb["v_mean3d"], pb["v_scale"], pb["v_quat"],
+                                                   rb["v_colors"], rb["v_opacity"])):
+                acc += g
+        return loss, [g for sc in grads for g in sc]
 
     def upload(self):
         for k, v in self.host.items():
@@ -316,6 +461,91 @@ def whole_job_ms_per_step(total_ms: float, steps: int, world: int) -> float:
     return total_ms / (steps * world)
 
 
+def add_stages_and_roofline(line, st, steps, flush):
+    stage_ms = time_stages(st, max(3, steps // 5), flush)
+    line["stages_ms"] = {k: round(v, 4) for k, v in stage_ms.items()}
+    line["num_intersects"] = st.count
+    stage_ms.pop("end", None)
+    dominant = max(stage_ms, key=stage_ms.get)
+    bytes_by_stage = st.stage_bytes()
+    peak, src = _peaks()
+    achieved = bytes_by_stage[dominant] / (stage_ms[dominant] * 1e-3) / 1e9
+    line["roofline"] = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1),
+                        "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                        "peak_source": src, "traffic": NCU_TRAFFIC.get(dominant),
+                        "algorithmic_bytes": bytes_by_stage[dominant]}
+
+
+BATCH_METRIC = "batched fwd+bwd ms/iter, 4 scenes x 8 views"
+
+
+def main_batch(a, torch, world, rank, local, dist, dev):
+    """--scene batch: the multi-scene, multi-view workload (one line)."""
+    from jaxsplat_gb300.scenes import BATCH_POINTS, BATCH_SIZES
+
+    config = {"workload": "batch: 4 scenes (" + ", ".join(str(n) for n in BATCH_POINTS)
+                          + " Gaussians) x 8 views each, image sizes "
+                          + "/".join(f"{w}x{h}" for h, w in BATCH_SIZES)
+                          + " mixed, fp32, fwd+bwd with per-view L2 loss",
+              "scenes": list(BATCH_POINTS), "views_per_scene": 8,
+              "l2": "flushed before every timed step",
+              "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import ref
+
+        if not ref.available():
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "reference kernels (oracle/_ref) not built on this machine"}))
+            return
+        st = RefBatchStep(a.seed, dev)
+    else:
+        st = BatchStep(a.seed, dev, graph=not a.no_graph, autotune=a.autotune,
+                       log=lambda m: print(m, file=sys.stderr))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        total = time_device(st, a.steps, a.warmup, flush)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total = max_over_ranks(total, dist, dev)
+    e2e_ms, bi, bo = time_e2e(st, max(3, a.steps // 2), flush)
+    e2e_ms = max_over_ranks(e2e_ms, dist, dev)
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    value = whole_job_ms_per_step(total, a.steps, world)
+    line = {"metric": BATCH_METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(total / a.steps, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": config,
+            "e2e": {"value": round(e2e_ms / world, 4), "unit": UNIT, "h2d_bytes_per_step": bi,
+                    "d2h_bytes_per_step": bo},
+            "clocks": clk.summary()}
+    if a.impl == "reference":
+        line["impl"] = "reference"
+        line["reference_kind"] = ("reference CUDA kernels built from its sources (oracle/_ref), "
+                                  "one render call per view, same GPU")
+        line["gpu_launches"] = None
+    else:
+        st.sess.check()
+        line["gpu_launches"] = st.launches_per_step() * a.steps
+        line["cuda_graph"] = st.graph
+        line["block_size"], line["chunk"] = st.sess.bw, st.sess.chunk
+        if st.tuning:
+            line["autotune_ms"] = {f"bw{k[0]}_chunk{k[1]}": round(v, 3) for k, v in st.tuning.items()}
+        b = st.sess.batch
+        line["entries"], line["tiles"], line["pixels"] = int(b.num_entries), int(b.num_tiles), int(b.num_pixels)
+        add_stages_and_roofline(line, st, a.steps, flush)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -326,6 +556,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-graph", action="store_true", help="eager launches instead of a CUDA graph")
+    ap.add_argument("--autotune", action="store_true",
+                    help="batch scene: sweep block size x scheduler chunk before timing")
     a = ap.parse_args()
     assert a.warmup >= 3, "at least 3 warm-up steps"
 
@@ -344,6 +576,8 @@ def main():
 
     from jaxsplat_gb300.scenes import make_scene
 
+    if a.scene == "batch":
+        return main_batch(a, torch, world, rank, local, dist, dev)
     sc = make_scene(a.scene, seed=a.seed)
     config = {"workload": f"{sc.spec.name}: {sc.spec.num_points} Gaussians, "
                           f"{sc.spec.img_shape[1]}x{sc.spec.img_shape[0]}, block 16, fp32, "
@@ -406,33 +640,7 @@ def main():
         st.sess.check()  # no step overflowed its capacity, no device check fired
         line["gpu_launches"] = st.launches_per_step() * a.steps
         line["cuda_graph"] = st.graph
-        count = st.count
-        h, w = sc.spec.img_shape
-        P = h * w
-        stage_ms = time_stages(st, max(3, a.steps // 5), flush)
-        line["stages_ms"] = {k: round(v, 4) for k, v in stage_ms.items()}
-        line["num_intersects"] = count
-        dominant = max(stage_ms, key=stage_ms.get)
-        # algorithmic bytes per launch: raster backward gathers 40 B per
-        # intersection (4 B id + the 36 B of xy, conic, opacity and color it
-        # uses), issues 9 fp32 atomics (36 B) per (tile, Gaussian) pair, and
-        # reads 24 B per pixel (final_Ts, final_idx, v_img, v_img_alpha); the
-        # forward stage adds the packing pass (36 B in + 48 B out per Gaussian).
-        n = sc.spec.num_points
-        bytes_by_stage = {"raster_bwd": 76 * count + 24 * P,
-                          "raster_fwd": 40 * count + 20 * P + 84 * n,
-                          "sort": 16 * n * 4 + 28 * n + 8 * count + 16 * count * st.passes,
-                          "project_fwd": 100 * sc.spec.num_points,
-                          "project_bwd": 140 * sc.spec.num_points,
-                          "l2_loss": 36 * P}
-        stage_ms.pop("end", None)
-        peak, src = _peaks()
-        achieved = bytes_by_stage[dominant] / (stage_ms[dominant] * 1e-3) / 1e9
-        traffic = NCU_TRAFFIC.get(dominant)
-        line["roofline"] = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1),
-                            "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                            "peak_source": src, "traffic": traffic,
-                            "algorithmic_bytes": bytes_by_stage[dominant]}
+        add_stages_and_roofline(line, st, a.steps, flush)
         if not a.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc)
     print(json.dumps(line))

@@ -259,6 +259,127 @@ SPLAT_API int splat_project_fwd_noalloc(const splat_params *p, const float *mean
                                         splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Batched render: many views of several scenes (uneven Gaussian counts and
+ * image sizes) in one pass of each kernel.  No counterpart in the reference,
+ * which renders one view per call (jaxsplat/__init__.py:6-70); every view's
+ * image, final_Ts and gradients equal those of that view rendered alone
+ * through the single-view entry points, and its final_idx too, shifted by
+ * the number of intersections of the views before it (final_idx indexes the
+ * batch's sorted list).  A view with no intersection at all keeps
+ * final_Ts = 1 (the single-view call's empty-list path writes 0).
+ *
+ * Scenes are concatenated: scene s owns Gaussians [scene_base[s],
+ * scene_base[s] + scene_points[s]) of the scene arrays (means3d (G,3),
+ * scales (G,3), quats (G,4), colors (G,3), opacities (G,1)).  An "entry" is
+ * one (view, Gaussian) pair; view v's entries start at a multiple of 256 and
+ * the per-entry arrays (cov3d, xys, depths, radii, conics, compensation,
+ * packed records, v_xy, v_conic) have num_entries rows, padding rows
+ * included (written as culled Gaussians).  Tiles and pixels are numbered
+ * view after view: view v's tile (tx, ty) is tile_base + ty*tiles_x + tx and
+ * its pixel (y, x) is pixel_base + y*width + x of the pixel buffers (img
+ * (P,3), final_Ts (P,1), final_idx (P,1), target, v_img, v_img_alpha).
+ *
+ * Fill each view's first block of fields, call splat_batch_layout on the
+ * host array (it fills the derived fields and the totals), copy the array to
+ * the device and point splat_batch::views at it. */
+typedef struct splat_view {
+    float viewmat[16];   /* row-major world -> camera */
+    float fx, fy, cx, cy;
+    float background[3];
+    uint32_t scene;
+    uint32_t img_height, img_width;
+    /* derived by splat_batch_layout */
+    uint32_t tiles_x, tiles_y;
+    uint32_t gauss_base;  /* first Gaussian of the view's scene */
+    uint32_t num_points;  /* the scene's Gaussian count */
+    uint32_t entry_base;  /* first entry of the view (multiple of 256) */
+    uint32_t tile_base;   /* first tile of the view */
+    uint64_t pixel_base;  /* first pixel of the view */
+} splat_view;
+
+typedef struct splat_batch {
+    uint32_t num_scenes, num_views;
+    float glob_scale, clip_thresh;
+    uint32_t block_width;          /* 2..16, shared by all views */
+    uint32_t *device_status;       /* as in splat_params */
+    uint32_t spin_limit;
+    const splat_view *views;       /* device array of num_views */
+    /* totals, derived by splat_batch_layout */
+    uint64_t num_points;           /* Gaussians over all scenes */
+    uint64_t num_entries, num_tiles, num_pixels;
+} splat_batch;
+
+/* Host: fills the derived fields of views[0..num_views) and b's totals from
+ * scene_points[0..num_scenes) (the scenes' Gaussian counts; scene s starts at
+ * the sum of the counts before it). */
+SPLAT_API int splat_batch_layout(splat_batch *b, splat_view *views, const uint32_t *scene_points);
+
+/* Projection forward of every entry (forward.cu:13-131 per view; tile counts
+ * are not kept).  total_dev (device int64) receives the number of
+ * intersections over all views; it is overwritten. */
+SPLAT_API int splat_batch_project_fwd(const splat_batch *b, const float *means3d,
+                                      const float *scales, const float *quats, float *cov3d,
+                                      float *xys, float *depths, int32_t *radii, float *conics,
+                                      float *compensation, int64_t *total_dev,
+                                      splat_stream_t stream);
+
+/* Sort and bin over all views, plus the order in which the rasterizers'
+ * persistent blocks take tiles (longest tile list first).  capacity and
+ * count_dev as for splat_sort_and_bin with a device count.
+ *   -> gaussian_ids_sorted (capacity,) int32 entry ids, tile_bins (num_tiles,2),
+ *      tile_order (num_tiles,) int32 */
+SPLAT_API size_t splat_batch_sort_workspace_size(const splat_batch *b, int64_t capacity);
+SPLAT_API int splat_batch_sort_and_bin(const splat_batch *b, int64_t capacity,
+                                       const int64_t *count_dev, const float *xys,
+                                       const float *depths, const int32_t *radii,
+                                       int32_t *gaussian_ids_sorted, int32_t *tile_bins,
+                                       int32_t *tile_order, void *workspace,
+                                       size_t workspace_bytes, splat_stream_t stream);
+
+/* Packed records of every entry (splat_pack_splats, with the colors and
+ * opacities of the entry's scene Gaussian). */
+SPLAT_API int splat_batch_pack(const splat_batch *b, const float *xys, const float *conics,
+                               const float *colors, const float *opacities, float *packed,
+                               splat_stream_t stream);
+
+/* Rasterize forward / backward over all views with persistent blocks that
+ * take `chunk` tiles at a time from tile_order (1..64).  The backward
+ * overwrites v_colors (G,3) and v_opacity (G,1) (summed over the views of
+ * each scene) and v_xy (E,2), v_conic (E,3) (per entry). */
+SPLAT_API int splat_batch_rasterize_fwd(const splat_batch *b, int64_t capacity,
+                                        const int64_t *count_dev,
+                                        const int32_t *gaussian_ids_sorted,
+                                        const int32_t *tile_bins, const int32_t *tile_order,
+                                        const float *packed, float *final_Ts, int32_t *final_idx,
+                                        float *out_img, uint32_t chunk, int32_t *work_counter,
+                                        splat_stream_t stream);
+SPLAT_API int splat_batch_rasterize_bwd(const splat_batch *b, int64_t capacity,
+                                        const int64_t *count_dev,
+                                        const int32_t *gaussian_ids_sorted,
+                                        const int32_t *tile_bins, const int32_t *tile_order,
+                                        const float *packed, const float *final_Ts,
+                                        const int32_t *final_idx, const float *v_img,
+                                        const float *v_img_alpha, float *v_colors,
+                                        float *v_opacity, float *v_xy, float *v_conic,
+                                        uint32_t chunk, int32_t *work_counter,
+                                        splat_stream_t stream);
+
+/* Sum over views of mean((img - target)^2) and its cotangent, per view
+ * v_img = 2 (img - target) / (3 H W).  loss_out is overwritten. */
+SPLAT_API int splat_batch_l2_loss(const splat_batch *b, const float *img, const float *target,
+                                  float *loss_out, float *v_img, splat_stream_t stream);
+
+/* Projection backward of every entry; the gradients of the scene arrays are
+ * summed over the views of each scene.  Overwrites v_mean3d (G,3),
+ * v_scale (G,3), v_quat (G,4). */
+SPLAT_API int splat_batch_project_bwd(const splat_batch *b, const float *means3d,
+                                      const float *scales, const float *quats,
+                                      const float *cov3d, const int32_t *radii,
+                                      const float *conics, const float *compensation,
+                                      const float *v_xy, const float *v_conic, float *v_mean3d,
+                                      float *v_scale, float *v_quat, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Self-test of the bounded wait: one block waits on a flag that nothing
  * sets, with `limit` polls, then records DEV_LOOKBACK_TIMEOUT in *status_dev
  * (device uint32) and returns.  Exists so the timeout path can be exercised

@@ -34,6 +34,37 @@ class SplatParams(C.Structure):
     ]
 
 
+class SplatView(C.Structure):
+    """Mirror of ``splat_view`` (include/splat.h)."""
+
+    _fields_ = [
+        ("viewmat", C.c_float * 16),
+        ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+        ("background", C.c_float * 3),
+        ("scene", C.c_uint32),
+        ("img_height", C.c_uint32), ("img_width", C.c_uint32),
+        ("tiles_x", C.c_uint32), ("tiles_y", C.c_uint32),
+        ("gauss_base", C.c_uint32), ("num_points", C.c_uint32),
+        ("entry_base", C.c_uint32), ("tile_base", C.c_uint32),
+        ("pixel_base", C.c_uint64),
+    ]
+
+
+class SplatBatch(C.Structure):
+    """Mirror of ``splat_batch`` (include/splat.h)."""
+
+    _fields_ = [
+        ("num_scenes", C.c_uint32), ("num_views", C.c_uint32),
+        ("glob_scale", C.c_float), ("clip_thresh", C.c_float),
+        ("block_width", C.c_uint32),
+        ("device_status", C.c_void_p),
+        ("spin_limit", C.c_uint32),
+        ("views", C.c_void_p),
+        ("num_points", C.c_uint64),
+        ("num_entries", C.c_uint64), ("num_tiles", C.c_uint64), ("num_pixels", C.c_uint64),
+    ]
+
+
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "workspace too small",
           4: "intersection count out of range", 5: "device-side check failed"}
 
@@ -67,6 +98,19 @@ _SIGS = [
     ("splat_project_fwd_noalloc", C.c_int, [_P] + [_v] * 13 + [_v]),
     ("splat_fit_transform", C.c_int, [C.c_int] + [_v] * 6 + [_v]),
     ("splat_fit_adam", C.c_int, [C.c_int, C.c_float] + [_v] * 16 + [_v]),
+    ("splat_batch_layout", C.c_int, [C.POINTER(SplatBatch), C.POINTER(SplatView),
+                                     C.POINTER(C.c_uint32)]),
+    ("splat_batch_project_fwd", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 10 + [_v]),
+    ("splat_batch_sort_workspace_size", C.c_size_t, [C.POINTER(SplatBatch), C.c_int64]),
+    ("splat_batch_sort_and_bin", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 7
+     + [_v, C.c_size_t, _v]),
+    ("splat_batch_pack", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 5 + [_v]),
+    ("splat_batch_rasterize_fwd", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 8
+     + [C.c_uint32, _v, _v]),
+    ("splat_batch_rasterize_bwd", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 13
+     + [C.c_uint32, _v, _v]),
+    ("splat_batch_l2_loss", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 4 + [_v]),
+    ("splat_batch_project_bwd", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 12 + [_v]),
 ]
 
 EXPORTED = [name for name, _, _ in _SIGS]

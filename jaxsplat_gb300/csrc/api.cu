@@ -83,6 +83,7 @@ static int check_count(long long count) {
     } while (0)
 
 static size_t project_ws_bytes(const splat_params &p) {
+    // one look-back word per partition (4096 Gaussians; sized per 256)
     const size_t parts = (p.num_points + 255) / 256;
     return (parts + 2) * sizeof(unsigned long long) + 256;
 }

@@ -29,8 +29,9 @@ int launch_project_fwd(const splat_params &, const float *, const float *, const
 int check_params(const splat_params *p);
 
 constexpr uint32_t kNoAllocMaxPoints = 1u << 24;
-// word 0: partition ticket; words 1..P: one look-back word per 256-Gaussian
-// partition; last word: the 64-bit intersection total when the caller
+// word 0: partition ticket; words 1..P: one look-back word per partition of
+// the projection (4096 Gaussians; the array allows one per 256, so it never
+// runs short); last word: the 64-bit intersection total when the caller
 // passes no total_out.
 constexpr size_t kNoAllocWords = 1 + (kNoAllocMaxPoints + 255) / 256 + 1;
 

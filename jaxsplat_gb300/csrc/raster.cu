@@ -26,6 +26,8 @@
 //    them, instead of one per warp.
 #include <math_constants.h>
 
+#include <algorithm>
+
 #include "splat_internal.cuh"
 #include "splat_math.cuh"
 
@@ -39,7 +41,9 @@ constexpr int kMaxWarps = kMaxTile / 32;
 //
 // Record (3 x float4):  r0 = (x, y, conic a, conic b)
 //                       r1 = (conic c, opacity, red, green)
-//                       r2 = (blue, hx, hy, 0)
+//                       r2 = (blue, hx, hy, tag)
+// (tag: 0 for a single view; for batched views the scene Gaussian's index,
+// as int bits, that receives the colour and opacity gradients.)
 // Outside the box |px - x| <= hx, |py - y| <= hy no pixel centre passes the
 // test alpha >= 1/255 in the rasterizers' fp32 arithmetic.  hx = +inf means
 // "no bound proven" (never culled); hx = -inf means "no pixel anywhere".
@@ -68,15 +72,13 @@ struct PackArgs {
     float4 *rec;
 };
 
-__global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const float2 xy = *reinterpret_cast<const float2 *>(a.xys + 2 * (size_t)i);
-    const float ca = a.conics[3 * (size_t)i], cb = a.conics[3 * (size_t)i + 1],
-                cc = a.conics[3 * (size_t)i + 2];
-    const float o = a.opac[i];
-    const float cr = a.colors[3 * (size_t)i], cg = a.colors[3 * (size_t)i + 1],
-                cbl = a.colors[3 * (size_t)i + 2];
+// Record of entry i whose colour and opacity are those of Gaussian gc; the
+// last word carries gc (as int bits) for the batched backward.
+__device__ __forceinline__ void pack_record(const PackArgs &a, size_t i, size_t gc, float tag) {
+    const float2 xy = *reinterpret_cast<const float2 *>(a.xys + 2 * i);
+    const float ca = a.conics[3 * i], cb = a.conics[3 * i + 1], cc = a.conics[3 * i + 2];
+    const float o = a.opac[gc];
+    const float cr = a.colors[3 * gc], cg = a.colors[3 * gc + 1], cbl = a.colors[3 * gc + 2];
     float hx = CUDART_INF_F, hy = CUDART_INF_F;
     // det = a c - b^2 (Kahan): w = b*b rounded, e = its rounding error
     const float w = cb * cb;
@@ -99,10 +101,36 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
             }
         }
     }
-    float4 *r = a.rec + 3 * (size_t)i;
+    float4 *r = a.rec + 3 * i;
     r[0] = make_float4(xy.x, xy.y, ca, cb);
     r[1] = make_float4(cc, o, cr, cg);
-    r[2] = make_float4(cbl, hx, hy, 0.f);
+    r[2] = make_float4(cbl, hx, hy, tag);
+}
+
+__global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    pack_record(a, (size_t)i, (size_t)i, 0.f);
+}
+
+// Batched views: entry i of view v packs Gaussian gauss_base + (i -
+// entry_base) of its scene; padding entries (past the scene's count) get a
+// record that no pixel passes.
+__global__ void __launch_bounds__(256) pack_batch_kernel(PackArgs a, const splat_view *views,
+                                                         int nviews) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const splat_view &v = views[view_by_entry(views, nviews, (uint32_t)i)];
+    const uint32_t k = (uint32_t)i - v.entry_base;
+    if (k < v.num_points) {
+        const uint32_t gc = v.gauss_base + k;
+        pack_record(a, (size_t)i, gc, __int_as_float((int)gc));
+    } else {
+        float4 *r = a.rec + 3 * (size_t)i;
+        r[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r[2] = make_float4(0.f, -CUDART_INF_F, -CUDART_INF_F, __int_as_float((int)v.gauss_base));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -185,6 +213,31 @@ __device__ __forceinline__ int warp_list(const unsigned *mask, int t0, int n, in
 }
 
 // ---------------------------------------------------------------------------
+// Where a tile's pixels live.  Single-view launches take the tile from the
+// block index; batched launches take it from a work list and the view table.
+
+struct TileCtx {
+    int tile;               // index into the tile bins
+    unsigned ox, oy;        // pixel origin of the tile within its image
+    unsigned width, height; // image size
+    size_t pix_base;        // first pixel of the image in the pixel buffers
+    float3 bg;
+};
+
+__device__ __forceinline__ TileCtx grid_tile(unsigned tiles_x, unsigned bw, unsigned width,
+                                             unsigned height, const float *background) {
+    TileCtx c;
+    c.tile = (int)(blockIdx.y * tiles_x + blockIdx.x);
+    c.ox = blockIdx.x * bw;
+    c.oy = blockIdx.y * bw;
+    c.width = width;
+    c.height = height;
+    c.pix_base = 0;
+    c.bg = make_float3(background[0], background[1], background[2]);
+    return c;
+}
+
+// ---------------------------------------------------------------------------
 // Forward.
 
 struct RasterFwdArgs {
@@ -202,14 +255,14 @@ struct RasterFwdArgs {
 };
 
 template <bool k8x4>
-__global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
+__device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &c) {
     __shared__ float4 s_r0[kMaxTile];
     __shared__ float4 s_r1[kMaxTile];
     __shared__ float s_blue[kMaxTile];
     __shared__ unsigned s_mask[kMaxTile];
     __shared__ float4 s_rect[kMaxWarps];
     __shared__ uint8_t s_list[kMaxWarps][kMaxTile];
-    const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
+    const int tile = c.tile;
     const int tr = threadIdx.x;
     const int bsize = a.bw * a.bw;
     const int lane = tr & 31, warp = tr >> 5, nwarps = (bsize + 31) >> 5;
@@ -217,13 +270,13 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
                                                                 : 0xffffffffu;
     int tx, ty;
     pixel_of<k8x4>(tr, a.bw, tx, ty);
-    const unsigned i = blockIdx.y * a.bw + ty;
-    const unsigned j = blockIdx.x * a.bw + tx;
+    const unsigned i = c.oy + ty;
+    const unsigned j = c.ox + tx;
     const float px = (float)j + 0.5f;
     const float py = (float)i + 0.5f;
-    const bool inside = i < a.height && j < a.width;
-    const size_t pix = (size_t)i * a.width + j;
-    const float3 bg = make_float3(a.background[0], a.background[1], a.background[2]);
+    const bool inside = i < c.height && j < c.width;
+    const size_t pix = c.pix_base + (size_t)i * c.width + j;
+    const float3 bg = c.bg;
 
     if (a.count.get() == 0) {  // lib/ops.cu:119-127: background image, zero T and index
         if (inside) {
@@ -235,9 +288,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
         }
         return;
     }
-    if (tr < nwarps)
-        s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)(blockIdx.x * a.bw),
-                                     (float)(blockIdx.y * a.bw));
+    if (tr < nwarps) s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
     const int2 range = a.bins[tile];
     bool done = !inside;
     float T = 1.f;
@@ -292,6 +343,11 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
         a.img[3 * pix + 1] = blend(acc.y, T, bg.y);
         a.img[3 * pix + 2] = blend(acc.z, T, bg.z);
     }
+}
+
+template <bool k8x4>
+__global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
+    fwd_tile<k8x4>(a, grid_tile(a.tiles_x, a.bw, a.width, a.height, a.background));
 }
 
 // ---------------------------------------------------------------------------
@@ -351,35 +407,39 @@ struct RasterBwdArgs {
     float *v_colors, *v_opac, *v_xy, *v_xy_abs, *v_conic;
 };
 
-template <bool kAbs>
-__global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
+// kScene: the color and opacity gradients go to the Gaussian whose index the
+// record carries in r2.w (batched views of shared scenes) instead of the list
+// entry's own index.
+template <bool kAbs, bool kScene>
+__device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &c) {
     constexpr bool k8x4 = false;  // other tile widths: row-major pixels
     __shared__ float4 s_r0[kMaxTile];
     __shared__ float4 s_r1[kMaxTile];
     __shared__ float s_blue[kMaxTile];
     __shared__ unsigned s_mask[kMaxTile];
     __shared__ int s_gid[kMaxTile];
+    __shared__ int s_cidx[kScene ? kMaxTile : 1];
     __shared__ float s_acc[kMaxTile][G_FIELDS];
     __shared__ int s_touched[kMaxTile];
     __shared__ int s_wmax[kMaxWarps];
     __shared__ float4 s_rect[kMaxWarps];
     __shared__ uint8_t s_list[kMaxWarps][kMaxTile];
 
-    const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
+    const int tile = c.tile;
     const int tr = threadIdx.x;
     const int bsize = a.bw * a.bw;
     const int lane = tr & 31, warp = tr >> 5, nwarps = (bsize + 31) >> 5;
     int tx, ty;
     pixel_of<k8x4>(tr, a.bw, tx, ty);
-    const unsigned i = blockIdx.y * a.bw + ty;
-    const unsigned j = blockIdx.x * a.bw + tx;
+    const unsigned i = c.oy + ty;
+    const unsigned j = c.ox + tx;
     const float px = (float)j + 0.5f;
     const float py = (float)i + 0.5f;
-    const bool inside = i < a.height && j < a.width;
+    const bool inside = i < c.height && j < c.width;
     // backward.cu:184: out-of-image threads read the last pixel
-    const size_t npix = (size_t)a.width * a.height;
-    const size_t pix = min((size_t)i * a.width + j, npix - 1);
-    const float3 bg = make_float3(a.background[0], a.background[1], a.background[2]);
+    const size_t npix = (size_t)c.width * c.height;
+    const size_t pix = c.pix_base + min((size_t)i * c.width + j, npix - 1);
+    const float3 bg = c.bg;
 
     if (a.count.get() == 0) return;  // lib/ops.cu:184-186: gradients stay zero
     const float T_final = a.final_Ts[pix];
@@ -396,9 +456,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                                                                 : 0xffffffffu;
     const int warp_bin_final = __reduce_max_sync(wmask, bin_final);
     if (lane == 0) s_wmax[warp] = warp_bin_final;
-    if (tr < nwarps)
-        s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)(blockIdx.x * a.bw),
-                                     (float)(blockIdx.y * a.bw));
+    if (tr < nwarps) s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
     __syncthreads();
     int block_max = 0;
     for (int w = 0; w < nwarps; ++w) block_max = max(block_max, s_wmax[w]);
@@ -415,6 +473,7 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
                 const float4 r1 = a.rec[3 * (size_t)g + 1];
                 const float4 r2 = a.rec[3 * (size_t)g + 2];
                 s_gid[tr] = g;
+                if (kScene) s_cidx[tr] = __float_as_int(r2.w);
                 s_r0[tr] = r0;
                 s_r1[tr] = r1;
                 s_blue[tr] = r2.x;
@@ -501,22 +560,28 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
         __syncthreads();
         if (idx >= range.x && s_touched[tr]) {
             const int g = s_gid[tr];
+            const int gc = kScene ? s_cidx[tr] : g;
             const float *acc = s_acc[tr];
-            atomicAdd(&a.v_colors[3 * (size_t)g + 0], acc[G_R]);
-            atomicAdd(&a.v_colors[3 * (size_t)g + 1], acc[G_G]);
-            atomicAdd(&a.v_colors[3 * (size_t)g + 2], acc[G_B]);
+            atomicAdd(&a.v_colors[3 * (size_t)gc + 0], acc[G_R]);
+            atomicAdd(&a.v_colors[3 * (size_t)gc + 1], acc[G_G]);
+            atomicAdd(&a.v_colors[3 * (size_t)gc + 2], acc[G_B]);
             atomicAdd(&a.v_conic[3 * (size_t)g + 0], acc[G_CA]);
             atomicAdd(&a.v_conic[3 * (size_t)g + 1], acc[G_CB]);
             atomicAdd(&a.v_conic[3 * (size_t)g + 2], acc[G_CC]);
             atomicAdd(&a.v_xy[2 * (size_t)g + 0], acc[G_X]);
             atomicAdd(&a.v_xy[2 * (size_t)g + 1], acc[G_Y]);
-            atomicAdd(&a.v_opac[g], acc[G_OP]);
+            atomicAdd(&a.v_opac[gc], acc[G_OP]);
             if (kAbs) {
                 atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], acc[G_AX]);
                 atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], acc[G_AY]);
             }
         }
     }
+}
+
+template <bool kAbs>
+__global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
+    bwd_tile<kAbs, false>(a, grid_tile(a.tiles_x, a.bw, a.width, a.height, a.background));
 }
 
 // ---------------------------------------------------------------------------
@@ -551,35 +616,36 @@ struct BwdPixel {
     float3 v_out;
 };
 
-template <bool kAbs>
-__global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs a) {
+template <bool kAbs, bool kScene>
+__device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx &c) {
     __shared__ float4 s_r0[kT16Batch];
     __shared__ float4 s_r1[kT16Batch];
     __shared__ float s_blue[kT16Batch];
     __shared__ unsigned s_mask[kT16Batch];
     __shared__ int s_gid[kT16Batch];
+    __shared__ int s_cidx[kScene ? kT16Batch : 1];
     __shared__ float s_acc[kT16Batch][G_FIELDS];
     __shared__ int s_touched[kT16Batch];
     __shared__ int s_wmax[kT16Warps];
     __shared__ float4 s_rect[kT16Warps];
     __shared__ uint8_t s_list[kT16Warps][kT16Batch];
 
-    const int tile = blockIdx.y * a.tiles_x + blockIdx.x;
+    const int tile = c.tile;
     const int tr = threadIdx.x, lane = tr & 31, warp = tr >> 5;
-    const unsigned j = blockIdx.x * 16 + ((warp & 1) << 3) + (lane & 7);
-    const unsigned i0 = blockIdx.y * 16 + ((warp >> 1) << 3) + (lane >> 3);
+    const unsigned j = c.ox + ((warp & 1) << 3) + (lane & 7);
+    const unsigned i0 = c.oy + ((warp >> 1) << 3) + (lane >> 3);
     const float px = (float)j + 0.5f;
     if (a.count.get() == 0) return;  // lib/ops.cu:184-186: gradients stay zero
-    const size_t npix = (size_t)a.width * a.height;
-    const float3 bg = make_float3(a.background[0], a.background[1], a.background[2]);
+    const size_t npix = (size_t)c.width * c.height;
+    const float3 bg = c.bg;
     BwdPixel P[2];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const unsigned i = i0 + 4 * q;
         P[q].py = (float)i + 0.5f;
-        P[q].inside = i < a.height && j < a.width;
+        P[q].inside = i < c.height && j < c.width;
         // backward.cu:184: out-of-image threads read the last pixel
-        const size_t pix = min((size_t)i * a.width + j, npix - 1);
+        const size_t pix = c.pix_base + min((size_t)i * c.width + j, npix - 1);
         const float T_final = a.final_Ts[pix];
         P[q].T = T_final;
         P[q].sv = 0.f;
@@ -591,7 +657,7 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
     const int2 range = a.bins[tile];
     const int warp_bin_final = __reduce_max_sync(0xffffffffu, max(P[0].bin_final, P[1].bin_final));
     if (lane == 0) s_wmax[warp] = warp_bin_final;
-    if (tr < kT16Warps) s_rect[tr] = warp_rect16(tr, (float)(blockIdx.x * 16), (float)(blockIdx.y * 16));
+    if (tr < kT16Warps) s_rect[tr] = warp_rect16(tr, (float)c.ox, (float)c.oy);
     __syncthreads();
     int block_max = 0;
 #pragma unroll
@@ -609,6 +675,7 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
                     const float4 r1 = a.rec[3 * (size_t)g + 1];
                     const float4 r2 = a.rec[3 * (size_t)g + 2];
                     s_gid[e] = g;
+                    if (kScene) s_cidx[e] = __float_as_int(r2.w);
                     s_r0[e] = r0;
                     s_r1[e] = r1;
                     s_blue[e] = r2.x;
@@ -709,16 +776,17 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
             const int idx = batch_end - e;
             if (idx >= range.x && s_touched[e]) {
                 const int g = s_gid[e];
+                const int gc = kScene ? s_cidx[e] : g;
                 const float *acc = s_acc[e];
-                atomicAdd(&a.v_colors[3 * (size_t)g + 0], acc[G_R]);
-                atomicAdd(&a.v_colors[3 * (size_t)g + 1], acc[G_G]);
-                atomicAdd(&a.v_colors[3 * (size_t)g + 2], acc[G_B]);
+                atomicAdd(&a.v_colors[3 * (size_t)gc + 0], acc[G_R]);
+                atomicAdd(&a.v_colors[3 * (size_t)gc + 1], acc[G_G]);
+                atomicAdd(&a.v_colors[3 * (size_t)gc + 2], acc[G_B]);
                 atomicAdd(&a.v_conic[3 * (size_t)g + 0], acc[G_CA]);
                 atomicAdd(&a.v_conic[3 * (size_t)g + 1], acc[G_CB]);
                 atomicAdd(&a.v_conic[3 * (size_t)g + 2], acc[G_CC]);
                 atomicAdd(&a.v_xy[2 * (size_t)g + 0], acc[G_X]);
                 atomicAdd(&a.v_xy[2 * (size_t)g + 1], acc[G_Y]);
-                atomicAdd(&a.v_opac[g], acc[G_OP]);
+                atomicAdd(&a.v_opac[gc], acc[G_OP]);
                 if (kAbs) {
                     atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], acc[G_AX]);
                     atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], acc[G_AY]);
@@ -726,6 +794,73 @@ __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs
             }
         }
     }
+}
+
+template <bool kAbs>
+__global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs a) {
+    bwd16_tile<kAbs, false>(a, grid_tile(a.tiles_x, 16, a.width, a.height, a.background));
+}
+
+// ---------------------------------------------------------------------------
+// Batched views: persistent blocks take `chunk` tiles at a time from a work
+// list (longest tile list first) through an atomic counter; each tile's view
+// comes from the view table.
+
+struct BatchTiles {
+    const int32_t *order;
+    int ntiles;
+    int chunk;
+    int *next;  // work counter, zero at launch
+    const splat_view *views;
+    int nviews;
+};
+
+__device__ __forceinline__ TileCtx view_tile(const BatchTiles &b, int tile, unsigned bw) {
+    const splat_view &v = b.views[view_by_tile(b.views, b.nviews, (uint32_t)tile)];
+    const unsigned local = (unsigned)tile - v.tile_base;
+    TileCtx c;
+    c.tile = tile;
+    c.ox = (local % v.tiles_x) * bw;
+    c.oy = (local / v.tiles_x) * bw;
+    c.width = v.img_width;
+    c.height = v.img_height;
+    c.pix_base = (size_t)v.pixel_base;
+    c.bg = make_float3(v.background[0], v.background[1], v.background[2]);
+    return c;
+}
+
+// Calls body(tile context) for every tile of the work list, with the block
+// synchronised between tiles.
+template <class Body>
+__device__ __forceinline__ void for_each_work_tile(const BatchTiles &b, unsigned bw, Body body) {
+    __shared__ int s_first;
+    for (;;) {
+        __syncthreads();  // the previous tile is done with shared memory
+        if (threadIdx.x == 0) s_first = atomicAdd(b.next, b.chunk);
+        __syncthreads();
+        const int first = s_first;
+        if (first >= b.ntiles) return;
+        const int last = min(first + b.chunk, b.ntiles);
+        for (int it = first; it < last; ++it) {
+            if (it > first) __syncthreads();
+            const int tile = b.order[it];
+            if (tile >= 0 && tile < b.ntiles) body(view_tile(b, tile, bw));
+        }
+    }
+}
+
+template <bool k8x4>
+__global__ void __launch_bounds__(kMaxTile) raster_fwd_batch_kernel(RasterFwdArgs a, BatchTiles b) {
+    for_each_work_tile(b, a.bw, [&](const TileCtx &c) { fwd_tile<k8x4>(a, c); });
+}
+
+__global__ void __launch_bounds__(kMaxTile) raster_bwd_batch_kernel(RasterBwdArgs a, BatchTiles b) {
+    for_each_work_tile(b, a.bw, [&](const TileCtx &c) { bwd_tile<false, true>(a, c); });
+}
+
+__global__ void __launch_bounds__(kT16Threads) raster_bwd16_batch_kernel(RasterBwdArgs a,
+                                                                          BatchTiles b) {
+    for_each_work_tile(b, 16, [&](const TileCtx &c) { bwd16_tile<false, true>(a, c); });
 }
 
 // ---------------------------------------------------------------------------
@@ -740,6 +875,100 @@ int launch_pack(const splat_params &p, const float *xys, const float *conics,
     if (a.n == 0) return SPLAT_OK;
     pack_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a);
     return check_launch("pack_kernel");
+}
+
+int launch_batch_pack(const splat_batch &b, const float *xys, const float *conics,
+                      const float *colors, const float *opac, float *rec, cudaStream_t s) {
+    PackArgs a;
+    a.n = (int)b.num_entries;
+    a.xys = xys; a.conics = conics; a.colors = colors; a.opac = opac;
+    a.rec = reinterpret_cast<float4 *>(rec);
+    if (a.n == 0) return SPLAT_OK;
+    pack_batch_kernel<<<(a.n + 255) / 256, 256, 0, s>>>(a, b.views, (int)b.num_views);
+    return check_launch("pack_batch_kernel");
+}
+
+// Resident blocks per SM times the SM count: the persistent grid.
+template <class K>
+static int persistent_grid(K kernel, int threads, int *grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess)
+        return check_launch("persistent grid query");
+    *grid = std::max(1, sms * std::max(1, per_sm));
+    return SPLAT_OK;
+}
+
+static BatchTiles batch_tiles(const splat_batch &b, const int32_t *order, int chunk, int *next) {
+    BatchTiles t;
+    t.order = order;
+    t.ntiles = (int)b.num_tiles;
+    t.chunk = chunk;
+    t.next = next;
+    t.views = b.views;
+    t.nviews = (int)b.num_views;
+    return t;
+}
+
+int launch_batch_raster_fwd(const splat_batch &b, Count count, const int32_t *ids,
+                            const int2 *bins, const int32_t *order, const float *rec,
+                            float *final_Ts, int32_t *final_idx, float *img, int chunk, int *next,
+                            cudaStream_t s) {
+    if (b.num_tiles == 0) return SPLAT_OK;
+    if (cudaMemsetAsync(next, 0, sizeof(int), s) != cudaSuccess)
+        return check_launch("work counter memset");
+    RasterFwdArgs a;
+    a.tiles_x = 0; a.width = 0; a.height = 0; a.bw = b.block_width;
+    a.n = (int)b.num_entries; a.status = b.device_status;
+    a.count = count; a.ids = ids; a.bins = bins;
+    a.rec = reinterpret_cast<const float4 *>(rec); a.background = nullptr;
+    a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
+    const BatchTiles t = batch_tiles(b, order, chunk, next);
+    const int threads = (int)(b.block_width * b.block_width);
+    int grid = 0;
+    if (b.block_width == 16) {
+        if (int rc = persistent_grid(raster_fwd_batch_kernel<true>, threads, &grid)) return rc;
+        raster_fwd_batch_kernel<true><<<grid, threads, 0, s>>>(a, t);
+    } else {
+        if (int rc = persistent_grid(raster_fwd_batch_kernel<false>, threads, &grid)) return rc;
+        raster_fwd_batch_kernel<false><<<grid, threads, 0, s>>>(a, t);
+    }
+    return check_launch("raster_fwd_batch_kernel");
+}
+
+int launch_batch_raster_bwd(const splat_batch &b, Count count, const int32_t *ids,
+                            const int2 *bins, const int32_t *order, const float *rec,
+                            const float *final_Ts, const int32_t *final_idx, const float *v_img,
+                            const float *v_alpha, float *v_colors, float *v_opac, float *v_xy,
+                            float *v_conic, int chunk, int *next, cudaStream_t s) {
+    const size_t g = b.num_points, e = b.num_entries;
+    if (cudaMemsetAsync(v_colors, 0, g * 3 * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(v_opac, 0, g * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(v_xy, 0, e * 2 * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(v_conic, 0, e * 3 * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(next, 0, sizeof(int), s) != cudaSuccess)
+        return check_launch("batch raster_bwd output memset");
+    if (count.cap == 0 || b.num_tiles == 0) return SPLAT_OK;
+    RasterBwdArgs a;
+    a.tiles_x = 0; a.width = 0; a.height = 0; a.bw = b.block_width;
+    a.n = (int)b.num_entries; a.status = b.device_status;
+    a.count = count; a.ids = ids; a.bins = bins;
+    a.rec = reinterpret_cast<const float4 *>(rec); a.background = nullptr;
+    a.final_Ts = final_Ts; a.final_idx = final_idx; a.v_img = v_img; a.v_alpha = v_alpha;
+    a.v_colors = v_colors; a.v_opac = v_opac; a.v_xy = v_xy; a.v_xy_abs = nullptr;
+    a.v_conic = v_conic;
+    const BatchTiles t = batch_tiles(b, order, chunk, next);
+    int grid = 0;
+    if (b.block_width == 16) {
+        if (int rc = persistent_grid(raster_bwd16_batch_kernel, kT16Threads, &grid)) return rc;
+        raster_bwd16_batch_kernel<<<grid, kT16Threads, 0, s>>>(a, t);
+        return check_launch("raster_bwd16_batch_kernel");
+    }
+    const int threads = (int)(b.block_width * b.block_width);
+    if (int rc = persistent_grid(raster_bwd_batch_kernel, threads, &grid)) return rc;
+    raster_bwd_batch_kernel<<<grid, threads, 0, s>>>(a, t);
+    return check_launch("raster_bwd_batch_kernel");
 }
 
 int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,

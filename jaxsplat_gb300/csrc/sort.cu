@@ -174,8 +174,8 @@ struct PassArgs {
 
 __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     __shared__ unsigned s_whist[kSortWarps][kRadix];  // per-warp digit counts -> exclusive offsets
-    __shared__ unsigned s_bstart[kRadix];             // block-local digit start
-    __shared__ unsigned s_gbase[kRadix];              // global position of the block's first key of digit
+    __shared__ int s_delta[kRadix];                   // block-local digit start, then global - local
+    __shared__ unsigned s_wsum[kSortWarps];
     __shared__ uint32_t s_keys[kPartKeys];
     __shared__ int32_t s_vals[kPartKeys];
     __shared__ int s_part;
@@ -185,19 +185,17 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     for (int i = lane; i < kRadix; i += 32) s_whist[warp][i] = 0u;
     __syncthreads();
     const int part = s_part;
-    const long long count = a.count.get();
-    if ((long long)part * kPartKeys >= count) return;  // past the end (capacity-sized grid)
+    // counts are at most 2^30 - 1 (checked on the host), so 32-bit indices
+    const int count = (int)a.count.get();
+    if (part * kPartKeys >= count) return;  // past the end (capacity-sized grid)
     // warp-striped: warp w owns keys [base, base + 32*items), item k of lane l
     // is key base + 32k + l, so (k, l) order is key order
-    const long long base = (long long)part * kPartKeys + (long long)warp * 32 * kSortItems;
+    const int base = part * kPartKeys + warp * 32 * kSortItems + lane;
 
     uint32_t key[kSortItems];
     unsigned rank[kSortItems];
 #pragma unroll
-    for (int k = 0; k < kSortItems; ++k) {
-        const long long idx = base + k * 32 + lane;
-        key[k] = idx < count ? a.keys_in[idx] : 0u;
-    }
+    for (int k = 0; k < kSortItems; ++k) key[k] = base + k * 32 < count ? a.keys_in[base + k * 32] : 0u;
     // Stable rank of each key among the warp's keys with the same digit:
     // the lanes holding a digit (match_any) are ranked by lane, and the
     // lowest of them adds their number to the warp's digit counter.  The
@@ -206,7 +204,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
-        const bool ok = base + k * 32 + lane < count;
+        const bool ok = base + k * 32 < count;
         const unsigned d = ok ? digit_of(key[k], a.shift, a.mask) : (unsigned)kRadix;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int leader = __ffs(peers) - 1;
@@ -217,7 +215,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     }
     __syncthreads();
 
-    // per digit (thread t = digit t): warp offsets, block count, look-back
+    // per digit (thread t = digit t): warp offsets, block count
     unsigned run = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) {
@@ -228,18 +226,20 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     const unsigned cnt = run;
     uint32_t *my = a.lookback + (size_t)part * kRadix + t;
     publish_word(my, (part == 0 ? kLbPrefix : kLbAgg) | (cnt & kLbMask));
-    // block-local exclusive scan of the digit counts (for staging)
-    s_bstart[t] = cnt;
-    __syncthreads();
-    for (int o = 1; o < kRadix; o <<= 1) {
-        const unsigned y = t >= o ? s_bstart[t - o] : 0u;
-        __syncthreads();
-        s_bstart[t] += y;
-        __syncthreads();
+    // block-local exclusive scan of the digit counts: warp scans + warp totals
+    unsigned incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
     }
-    const unsigned bstart = s_bstart[t] - cnt;
+    if (lane == 31) s_wsum[warp] = incl;
     __syncthreads();
-    s_bstart[t] = bstart;
+    unsigned wbase = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) wbase += w < warp ? s_wsum[w] : 0u;
+    const unsigned bstart = wbase + incl - cnt;
+    s_delta[t] = (int)bstart;
     __syncthreads();
 
     // stage in digit order; the values are loaded only now (coalesced, in
@@ -248,14 +248,13 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     for (int k = 0; k < kSortItems; ++k) {
         if (rank[k] != 0xffffffffu) {
             const unsigned d = digit_of(key[k], a.shift, a.mask);
-            rank[k] += s_bstart[d] + s_whist[warp][d];
+            rank[k] += (unsigned)s_delta[d] + s_whist[warp][d];
             if (rank[k] < (unsigned)kPartKeys) s_keys[rank[k]] = key[k];
         }
     }
 #pragma unroll
-    for (int k = 0; k < kSortItems; ++k) {
-        if (rank[k] < (unsigned)kPartKeys) s_vals[rank[k]] = a.vals_in[base + k * 32 + lane];
-    }
+    for (int k = 0; k < kSortItems; ++k)
+        if (rank[k] < (unsigned)kPartKeys) s_vals[rank[k]] = a.vals_in[base + k * 32];
     // look-back last, after the staging: the predecessors have had that long
     // to publish their prefixes, and the keys are out of registers
     unsigned excl = 0;
@@ -263,15 +262,16 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
         excl = lookback_digit(a.lookback + t, kRadix, part, a.spin_limit, a.status);
         publish_word(my, kLbPrefix | ((excl + cnt) & kLbMask));
     }
-    s_gbase[t] = a.offs[t] + excl;
+    __syncthreads();  // every thread has read s_delta for its staging
+    // staged position i of digit d goes to global position i + delta[d]
+    s_delta[t] = (int)(a.offs[t] + excl) - (int)bstart;
     __syncthreads();
-    const long long remaining = count - (long long)part * kPartKeys;
-    const int nvalid = remaining < kPartKeys ? (int)remaining : kPartKeys;
+    const int nvalid = min(count - part * kPartKeys, kPartKeys);
+#pragma unroll 4
     for (int i = t; i < nvalid; i += kSortThreads) {
         const uint32_t k = s_keys[i];
-        const unsigned d = digit_of(k, a.shift, a.mask);
-        const long long g = (long long)s_gbase[d] + (i - (int)s_bstart[d]);
-        if (g < 0 || g >= count) {
+        const int g = s_delta[digit_of(k, a.shift, a.mask)] + i;
+        if ((unsigned)g >= (unsigned)count) {
             raise_status(a.status, DEV_SORT_OVERFLOW);
             continue;
         }
@@ -310,8 +310,8 @@ static RadixBufs radix_layout(Arena &ar, long long count, int end_bit) {
 // Sorts (ka, va) by the low end_bit bits of the keys.  Returns the buffers
 // holding the result; the last pass writes the values to vals_final instead
 // when it is given.
-static int radix_sort(const splat_params &p, const RadixBufs &b, Count count, int end_bit,
-                      int32_t *vals_final, const uint32_t **keys_sorted,
+static int radix_sort(uint32_t *status, uint32_t spin, const RadixBufs &b, Count count,
+                      int end_bit, int32_t *vals_final, const uint32_t **keys_sorted,
                       const int32_t **vals_sorted, cudaStream_t s) {
     if (count.cap > (long long)kLbMask)
         return fail(SPLAT_ERR_OVERFLOW, "sort of %lld keys exceeds %u", count.cap, kLbMask);
@@ -343,8 +343,8 @@ static int radix_sort(const splat_params &p, const RadixBufs &b, Count count, in
         pa.offs = b.offs + d * kRadix;
         pa.lookback = b.lookback + (size_t)d * b.nparts * kRadix;
         pa.ticket = b.tickets + d;
-        pa.status = p.device_status;
-        pa.spin_limit = spin_limit(p);
+        pa.status = status;
+        pa.spin_limit = spin;
         onesweep_kernel<<<(unsigned)b.nparts, kSortThreads, 0, s>>>(pa);
         if (int rc = check_launch("onesweep_kernel")) return rc;
         kin = kout;
@@ -373,41 +373,72 @@ __global__ void depth_keys_kernel(int n, const float *depths, const int32_t *rad
 // Stage 2: emission in depth order, in two kernels.
 //
 // emit_offsets_kernel: each Gaussian's first slot, an exclusive scan of the
-// tile counts in depth order.  Large partitions (4096 positions per block,
-// 16 per thread) keep the look-back chain short: the decoupled look-back's
+// tile counts in depth order.  Large partitions (4096 positions per block of
+// 1024 threads) keep the look-back chain short: the decoupled look-back's
 // inclusive prefixes advance by one window of partitions per L2 round trip,
 // so its latency grows with the number of partitions.
 // emit_expand_kernel: a block owns 256 consecutive positions of the depth
 // order; their tile rectangles are expanded cooperatively so that
 // consecutive threads write consecutive slots.  No waiting on other blocks.
 
-constexpr int kEmitBlock = 256;
-constexpr int kOffItems = 16;
-constexpr int kOffPart = kEmitBlock * kOffItems;
+// The tile grid an entry is emitted into: one grid (single view), or the
+// grid of the entry's view, whose tiles are numbered from its tile_base
+// (batched views).
+struct SingleGrid {
+    unsigned tiles_x, tiles_y, bw;
+    __device__ __forceinline__ void of(int, unsigned &tx_n, unsigned &ty_n, unsigned &base) const {
+        tx_n = tiles_x;
+        ty_n = tiles_y;
+        base = 0;
+    }
+};
 
+struct ViewGrid {
+    const splat_view *views;
+    int nviews;
+    unsigned bw;
+    __device__ __forceinline__ void of(int entry, unsigned &tx_n, unsigned &ty_n,
+                                       unsigned &base) const {
+        const splat_view &v = views[view_by_entry(views, nviews, (uint32_t)entry)];
+        tx_n = v.tiles_x;
+        ty_n = v.tiles_y;
+        base = v.tile_base;
+    }
+};
+
+constexpr int kEmitBlock = 256;
+constexpr int kOffThreads = 1024;
+constexpr int kOffItems = 4;
+constexpr int kOffPart = kOffThreads * kOffItems;
+
+template <class Grid>
 struct EmitOffsetsArgs {
     int n;
     const int32_t *order;  // Gaussian ids in depth order
     const float *xys;
     const int32_t *radii;
-    unsigned tiles_x, tiles_y, bw;
+    Grid grid;
     int32_t *offs;              // [n] first slot of each depth position (saturated at INT32_MAX)
     unsigned long long *words;  // [0] ticket, [1 + b] look-back word of block b
     uint32_t *status;
     uint32_t spin_limit;
 };
 
-__device__ __forceinline__ int rect_count(const EmitOffsetsArgs &a, int g) {
+template <class Grid>
+__device__ __forceinline__ int rect_count(const EmitOffsetsArgs<Grid> &a, int g) {
     if (g < 0 || g >= a.n) return 0;
     const int rad = a.radii[g];
     if (rad <= 0) return 0;
+    unsigned tx_n, ty_n, base;
+    a.grid.of(g, tx_n, ty_n, base);
     const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
-    const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
+    const TileRect r = tile_rect(c, (float)rad, tx_n, ty_n, a.grid.bw);
     return (int)((r.x1 - r.x0) * (r.y1 - r.y0));
 }
 
-__global__ void __launch_bounds__(kEmitBlock) emit_offsets_kernel(EmitOffsetsArgs a) {
-    __shared__ unsigned long long s_warp[kEmitBlock / 32];
+template <class Grid>
+__global__ void __launch_bounds__(kOffThreads) emit_offsets_kernel(EmitOffsetsArgs<Grid> a) {
+    __shared__ unsigned long long s_warp[kOffThreads / 32];
     __shared__ unsigned long long s_base;
     __shared__ int s_part;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -433,14 +464,14 @@ __global__ void __launch_bounds__(kEmitBlock) emit_offsets_kernel(EmitOffsetsArg
     if (lane == 31) s_warp[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        unsigned long long w = lane < kEmitBlock / 32 ? s_warp[lane] : 0ull;
+        unsigned long long w = lane < kOffThreads / 32 ? s_warp[lane] : 0ull;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned long long u = __shfl_up_sync(0xffffffffu, w, o);
             if (lane >= o) w += u;
         }
-        if (lane < kEmitBlock / 32) s_warp[lane] = w;  // inclusive over warps
-        const unsigned long long block_total = __shfl_sync(0xffffffffu, w, kEmitBlock / 32 - 1);
+        if (lane < kOffThreads / 32) s_warp[lane] = w;  // inclusive over warps
+        const unsigned long long block_total = __shfl_sync(0xffffffffu, w, kOffThreads / 32 - 1);
         unsigned long long *words = a.words + 1;
         unsigned long long excl = 0;
         if (part == 0) {
@@ -462,41 +493,44 @@ __global__ void __launch_bounds__(kEmitBlock) emit_offsets_kernel(EmitOffsetsArg
     }
 }
 
+template <class Grid>
 struct EmitExpandArgs {
     int n;
     const int32_t *order;
     const int32_t *offs;
     const float *xys;
     const int32_t *radii;
-    unsigned tiles_x, tiles_y, bw;
+    Grid grid;
     Count count;
     uint32_t *tile_out;
     int32_t *id_out;
     uint32_t *status;
 };
 
-__global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs a) {
+template <class Grid>
+__global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs<Grid> a) {
     __shared__ int s_off[kEmitBlock];
-    __shared__ unsigned s_x0[kEmitBlock], s_y0[kEmitBlock], s_w[kEmitBlock];
-    __shared__ int s_gid[kEmitBlock];
+    __shared__ int4 s_info[kEmitBlock];  // (first tile, tiles per row of the grid, width, id)
+    __shared__ float s_rw[kEmitBlock];   // 1 / width
     __shared__ int s_total;
     const int t = threadIdx.x;
     const int k0 = blockIdx.x * kEmitBlock;
     const int k = k0 + t;
     const int last = min(a.n, k0 + kEmitBlock) - 1;
-    long long base = a.offs[k0];
+    const int base = a.offs[k0];
     int cnt = 0;
     if (k < a.n) {
         const int g = a.order[k];
         if (g >= 0 && g < a.n) {
             const int rad = a.radii[g];
             if (rad > 0) {
+                unsigned tx_n, ty_n, tbase;
+                a.grid.of(g, tx_n, ty_n, tbase);
                 const float2 c = make_float2(a.xys[2 * (size_t)g], a.xys[2 * (size_t)g + 1]);
-                const TileRect r = tile_rect(c, (float)rad, a.tiles_x, a.tiles_y, a.bw);
-                s_x0[t] = r.x0;
-                s_y0[t] = r.y0;
-                s_w[t] = r.x1 - r.x0;
-                s_gid[t] = g;
+                const TileRect r = tile_rect(c, (float)rad, tx_n, ty_n, a.grid.bw);
+                s_info[t] = make_int4((int)(tbase + r.y0 * tx_n + r.x0), (int)tx_n,
+                                      (int)(r.x1 - r.x0), g);
+                s_rw[t] = 1.f / (float)(r.x1 - r.x0);
                 cnt = (int)((r.x1 - r.x0) * (r.y1 - r.y0));
             }
         } else {
@@ -514,25 +548,29 @@ __global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs 
     const long long count = a.count.get();
     if (blockIdx.x == 0 && t == 0 && a.count.dev && *a.count.dev > a.count.cap)
         raise_status(a.status, DEV_CAPACITY);
-    for (int s = t; s < total; s += kEmitBlock) {
-        // owner: last j with s_off[j] <= s (skips Gaussians with no slots)
-        int lo = 0, hi = kEmitBlock - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_off[mid] <= s) lo = mid; else hi = mid - 1;
-        }
-        const int j = lo;
+    // slots past the count are not written (and reported once)
+    const int lim = (int)max(0ll, min((long long)total, count - (long long)base));
+    if (t == 0 && lim < total) raise_status(a.status, DEV_EMIT_OVERFLOW);
+    for (int s = t; s < lim; s += kEmitBlock) {
+        // owner: last j with s_off[j] <= s (skips Gaussians with no slots);
+        // s_off[0] = 0 <= s, so a fixed-depth search over 256 entries
+        int j = 0;
+#pragma unroll
+        for (int step = kEmitBlock / 2; step > 0; step >>= 1)
+            if (s_off[j + step] <= s) j += step;
         const int kk = s - s_off[j];
-        const unsigned w = s_w[j];
-        const unsigned ty = s_y0[j] + (unsigned)kk / w;
-        const unsigned tx = s_x0[j] + (unsigned)kk % w;
-        const long long slot = base + s;
-        if (slot >= count) {
-            raise_status(a.status, DEV_EMIT_OVERFLOW);
-            continue;
-        }
-        a.tile_out[slot] = ty * a.tiles_x + tx;
-        a.id_out[slot] = s_gid[j];
+        const int4 info = s_info[j];
+        const int w = info.z;
+        // kk / w through the float reciprocal, corrected to the exact
+        // quotient: the quotient is a row of the rectangle (below 2^16), so
+        // the estimate's relative error of ~2^-22 puts it off by at most one
+        int qy = (int)((float)kk * s_rw[j]);
+        int rx = kk - qy * w;
+        if (rx < 0) { --qy; rx += w; }
+        if (rx >= w) { ++qy; rx -= w; }
+        const int slot = base + s;
+        a.tile_out[slot] = (uint32_t)(info.x + qy * info.y + rx);
+        a.id_out[slot] = info.w;
     }
 }
 
@@ -721,30 +759,32 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
     const uint32_t *gkeys;
     const int32_t *order;
     const Count all{nullptr, n, n};
-    if (int rc = radix_sort(p, L.g, all, 32, nullptr, &gkeys, &order, s)) return rc;
+    if (int rc = radix_sort(p.device_status, spin_limit(p), L.g, all, 32, nullptr, &gkeys, &order, s))
+        return rc;
     // 2. emission in depth order
     const int oblocks = (n + kOffPart - 1) / kOffPart;
     if (cudaMemsetAsync(L.words, 0, sizeof(unsigned long long) * (size_t)(oblocks + 1), s) != cudaSuccess)
         return check_launch("emission workspace memset");
-    EmitOffsetsArgs eo;
+    const SingleGrid grid{tx, ty, p.block_width};
+    EmitOffsetsArgs<SingleGrid> eo;
     eo.n = n;
     eo.order = order;
     eo.xys = xys;
     eo.radii = radii;
-    eo.tiles_x = tx; eo.tiles_y = ty; eo.bw = p.block_width;
+    eo.grid = grid;
     eo.offs = L.offs;
     eo.words = L.words;
     eo.status = p.device_status;
     eo.spin_limit = spin_limit(p);
-    emit_offsets_kernel<<<oblocks, kEmitBlock, 0, s>>>(eo);
+    emit_offsets_kernel<<<oblocks, kOffThreads, 0, s>>>(eo);
     if (int rc = check_launch("emit_offsets_kernel")) return rc;
-    EmitExpandArgs e;
+    EmitExpandArgs<SingleGrid> e;
     e.n = n;
     e.order = order;
     e.offs = L.offs;
     e.xys = xys;
     e.radii = radii;
-    e.tiles_x = tx; e.tiles_y = ty; e.bw = p.block_width;
+    e.grid = grid;
     e.count = count;
     e.tile_out = L.s.ka;
     e.id_out = L.s.va;
@@ -755,7 +795,8 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
     const int tile_bits = std::max(1, bit_length(T - 1));
     const uint32_t *tiles_sorted;
     const int32_t *ids_final;
-    if (int rc = radix_sort(p, L.s, count, tile_bits, ids_sorted, &tiles_sorted, &ids_final, s))
+    if (int rc = radix_sort(p.device_status, spin_limit(p), L.s, count, tile_bits, ids_sorted,
+                            &tiles_sorted, &ids_final, s))
         return rc;
     if (keys_sorted_out) {
         compose_keys_kernel<<<(unsigned)((count.cap + 255) / 256), 256, 0, s>>>(
@@ -766,6 +807,121 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
     // 4. bins
     tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(tiles_sorted, count, (int)T, bins);
     return check_launch("tile_bins_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Batched views: the same pipeline over all entries of all views, tiles
+// numbered view after view, plus the rasterizers' work order.
+
+constexpr int kCostBits = 24;
+constexpr uint32_t kCostMask = (1u << kCostBits) - 1u;
+
+// Ascending keys put the longest tile lists first (lists longer than 2^24
+// share the first key).
+__global__ void tile_cost_kernel(const int2 *bins, int ntiles, uint32_t *keys, int32_t *vals) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    const int2 r = bins[t];
+    const unsigned cost = (unsigned)max(0, r.y - r.x);
+    keys[t] = kCostMask - min(cost, kCostMask);
+    vals[t] = t;
+}
+
+struct BatchSortLayout {
+    RadixBufs g;                // entries by depth
+    unsigned long long *words;  // emission look-back words
+    int32_t *offs;              // first slot of each depth position
+    RadixBufs s;                // intersections by tile
+    RadixBufs o;                // tiles by list length
+};
+
+static BatchSortLayout batch_sort_layout(Arena &ar, const splat_batch &b, long long count) {
+    BatchSortLayout L;
+    const long long e = (long long)b.num_entries, T = (long long)b.num_tiles;
+    L.g = radix_layout(ar, e, 32);
+    L.words = ar.take<unsigned long long>((size_t)((e + kOffPart - 1) / kOffPart + 1));
+    L.offs = ar.take<int32_t>((size_t)e);
+    L.s = radix_layout(ar, count, std::max(1, bit_length((unsigned)(T - 1))));
+    L.o = radix_layout(ar, T, kCostBits);
+    return L;
+}
+
+size_t batch_sort_workspace_bytes(const splat_batch &b, long long count) {
+    Arena ar{nullptr, 0};
+    batch_sort_layout(ar, b, count);
+    return ar.used + 256;
+}
+
+int launch_batch_sort_and_bin(const splat_batch &b, Count count, const float *xys,
+                              const float *depths, const int32_t *radii, int32_t *ids_sorted,
+                              int2 *bins, int32_t *order, void *ws, size_t ws_bytes,
+                              cudaStream_t s) {
+    const int e = (int)b.num_entries, T = (int)b.num_tiles;
+    Arena ar{static_cast<char *>(ws), ws_bytes};
+    const BatchSortLayout L = batch_sort_layout(ar, b, count.cap);
+    if (!ar.fits())
+        return fail(SPLAT_ERR_WORKSPACE, "batch sort workspace too small: need %zu bytes, got %zu",
+                    ar.used, ws_bytes);
+    const uint32_t spin = spin_limit(b);
+    if (count.cap > 0 && e > 0) {
+        // 1. entries by depth
+        depth_keys_kernel<<<(e + 255) / 256, 256, 0, s>>>(e, depths, radii, L.g.ka, L.g.va);
+        if (int rc = check_launch("depth_keys_kernel")) return rc;
+        const uint32_t *gkeys;
+        const int32_t *order_d;
+        const Count all{nullptr, e, e};
+        if (int rc = radix_sort(b.device_status, spin, L.g, all, 32, nullptr, &gkeys, &order_d, s))
+            return rc;
+        // 2. emission in depth order, each entry into its view's tiles
+        const int oblocks = (e + kOffPart - 1) / kOffPart;
+        if (cudaMemsetAsync(L.words, 0, sizeof(unsigned long long) * (size_t)(oblocks + 1), s) !=
+            cudaSuccess)
+            return check_launch("emission workspace memset");
+        const ViewGrid grid{b.views, (int)b.num_views, b.block_width};
+        EmitOffsetsArgs<ViewGrid> eo;
+        eo.n = e;
+        eo.order = order_d;
+        eo.xys = xys;
+        eo.radii = radii;
+        eo.grid = grid;
+        eo.offs = L.offs;
+        eo.words = L.words;
+        eo.status = b.device_status;
+        eo.spin_limit = spin;
+        emit_offsets_kernel<<<oblocks, kOffThreads, 0, s>>>(eo);
+        if (int rc = check_launch("emit_offsets_kernel")) return rc;
+        EmitExpandArgs<ViewGrid> ex;
+        ex.n = e;
+        ex.order = order_d;
+        ex.offs = L.offs;
+        ex.xys = xys;
+        ex.radii = radii;
+        ex.grid = grid;
+        ex.count = count;
+        ex.tile_out = L.s.ka;
+        ex.id_out = L.s.va;
+        ex.status = b.device_status;
+        emit_expand_kernel<<<(e + kEmitBlock - 1) / kEmitBlock, kEmitBlock, 0, s>>>(ex);
+        if (int rc = check_launch("emit_expand_kernel")) return rc;
+        // 3. stable sort by global tile id; 4. bins
+        const int tile_bits = std::max(1, bit_length((unsigned)(T - 1)));
+        const uint32_t *tiles_sorted;
+        const int32_t *ids_final;
+        if (int rc = radix_sort(b.device_status, spin, L.s, count, tile_bits, ids_sorted,
+                                &tiles_sorted, &ids_final, s))
+            return rc;
+        tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(tiles_sorted, count, T, bins);
+        if (int rc = check_launch("tile_bins_kernel")) return rc;
+    } else if (cudaMemsetAsync(bins, 0, sizeof(int2) * (size_t)T, s) != cudaSuccess) {
+        return check_launch("tile_bins memset");
+    }
+    // 5. work order: longest list first
+    tile_cost_kernel<<<(T + 255) / 256, 256, 0, s>>>(bins, T, L.o.ka, L.o.va);
+    if (int rc = check_launch("tile_cost_kernel")) return rc;
+    const uint32_t *ck;
+    const int32_t *cv;
+    const Count tiles{nullptr, T, T};
+    return radix_sort(b.device_status, spin, L.o, tiles, kCostBits, order, &ck, &cv, s);
 }
 
 }  // namespace splat

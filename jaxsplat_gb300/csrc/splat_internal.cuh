@@ -37,6 +37,28 @@ struct Count {
 
 constexpr uint32_t kDefaultSpinLimit = 1u << 22;
 
+// Batched views: the view that owns an entry, a tile or a pixel.  Views are
+// laid out in order, so every base field is non-decreasing over the table and
+// the owner is the last view whose base is <= the key.
+template <class Key, class Field>
+__device__ __forceinline__ int view_search(const splat_view *v, int n, Key key, Field field) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (field(v[mid]) <= key) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int view_by_entry(const splat_view *v, int n, uint32_t entry) {
+    return view_search(v, n, entry, [](const splat_view &x) { return x.entry_base; });
+}
+__device__ __forceinline__ int view_by_tile(const splat_view *v, int n, uint32_t tile) {
+    return view_search(v, n, tile, [](const splat_view &x) { return x.tile_base; });
+}
+__device__ __forceinline__ int view_by_pixel(const splat_view *v, int n, uint64_t pix) {
+    return view_search(v, n, pix, [](const splat_view &x) { return x.pixel_base; });
+}
+
 __device__ __forceinline__ void raise_status(uint32_t *status, uint32_t bits) {
     if (status) atomicOr(status, bits);
 }
@@ -117,6 +139,9 @@ inline unsigned n_tiles(const splat_params &p) { return tiles_x(p) * tiles_y(p);
 
 inline uint32_t spin_limit(const splat_params &p) {
     return p.spin_limit ? p.spin_limit : kDefaultSpinLimit;
+}
+inline uint32_t spin_limit(const splat_batch &b) {
+    return b.spin_limit ? b.spin_limit : kDefaultSpinLimit;
 }
 
 // Sets the thread-local error message and returns `code`.

@@ -111,3 +111,52 @@ def make_scene(spec: SceneSpec | str, seed: int = 0, num_points: int | None = No
         viewmat=np.eye(4, dtype=np.float32), background=np.asarray(spec.background, np.float32),
         target=target,
     )
+
+
+def look_at(eye, target=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Row-major world -> camera matrix of a camera at `eye` looking at
+    `target` (+z forward, +y down in the image, world +y as the down
+    direction, like the identity view matrix)."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    d = np.array([0.0, 1.0, 0.0])
+    r = np.cross(d, f)
+    r /= np.linalg.norm(r)
+    d = np.cross(f, r)
+    R = np.stack([r, d, f])
+    V = np.eye(4)
+    V[:3, :3] = R
+    V[:3, 3] = -R @ eye
+    return V.astype(np.float32)
+
+
+# The batched workload: 4 scenes (Gaussian counts below, distributions of the
+# "small" scene), 8 cameras per scene on a circle of radius 6 around the
+# origin looking at it, poses jittered by seed, image sizes cycling through
+# 512x512, 1280x720 and 1920x1080, f = 0.625 W (the 1920x1080 scene's
+# field of view), principal point at the centre.
+BATCH_POINTS = (50_000, 200_000, 800_000, 2_000_000)
+BATCH_SIZES = ((512, 512), (720, 1280), (1080, 1920))
+
+
+def make_batch(seed: int = 0, scene_points=BATCH_POINTS, views_per_scene: int = 8,
+               sizes=BATCH_SIZES, radius: float = 6.0):
+    """Returns (scenes, views, targets): scene dicts with means3d, scales,
+    quats, colors, opacities; view dicts with scene, viewmat, img_shape, f,
+    c, background; one U[0,1] target image per view."""
+    rng = np.random.default_rng(seed)
+    scenes, views, targets = [], [], []
+    for s, n in enumerate(scene_points):
+        sc = make_scene("small", seed=seed * 1000 + s, num_points=int(n))
+        scenes.append(dict(means3d=sc.means3d, scales=sc.scales, quats=sc.quats,
+                           colors=sc.colors, opacities=sc.opacities))
+        for v in range(views_per_scene):
+            th = 2.0 * np.pi * v / views_per_scene + rng.uniform(-0.1, 0.1)
+            eye = (radius * np.sin(th), rng.uniform(-0.3, 0.3), -radius * np.cos(th))
+            h, w = sizes[(s + v) % len(sizes)]
+            f = 0.625 * w
+            views.append(dict(scene=s, viewmat=look_at(eye), img_shape=(h, w), f=(f, f),
+                              c=(w / 2.0, h / 2.0), background=np.zeros(3, np.float32)))
+            targets.append(rng.uniform(0.0, 1.0, (h, w, 3)).astype(np.float32))
+    return scenes, views, targets

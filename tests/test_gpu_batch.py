@@ -1,0 +1,114 @@
+"""Batched multi-view, multi-scene render (BatchSession): every view's image,
+final_Ts and final_idx equal the single-view render of that view bit for bit;
+per-entry screen-space gradients equal the view's own; scene gradients equal
+the sum over the scene's views of the single-view gradients; graph replay
+equals eager; capacity overflow is reported."""
+
+import numpy as np
+import pytest
+
+from conftest import normwise_rel
+
+pytestmark = pytest.mark.gpu
+
+SIZES = ((48, 64), (80, 96), (70, 50), (33, 17))
+
+
+def _batch(bw, points=(3000, 5000), views_per_scene=3, seed=3):
+    from jaxsplat_gb300.batch import BatchSession
+    from jaxsplat_gb300.scenes import make_batch
+
+    scenes, views, targets = make_batch(seed, scene_points=points, views_per_scene=views_per_scene,
+                                        sizes=SIZES)
+    views[1]["background"] = np.array([0.2, 0.5, 0.9], np.float32)
+    bs = BatchSession(scenes, views, targets, block_size=bw)
+    return bs, scenes, views, targets
+
+
+def _single(scene, view, target, bw):
+    from jaxsplat_gb300.session import RenderSession
+
+    h, w = view["img_shape"]
+    n = scene["means3d"].shape[0]
+    s = RenderSession(n, img_shape=(h, w), f=view["f"], c=view["c"], glob_scale=1.0,
+                      clip_thresh=0.01, block_size=bw)
+    s.set_inputs(scene["means3d"], scene["scales"], scene["quats"], scene["colors"],
+                 scene["opacities"], view["viewmat"], view.get("background", np.zeros(3)), target)
+    s.measure_capacity()
+    s.step()
+    s.check()
+    return s
+
+
+@pytest.mark.parametrize("bw", [16, 8, 12])
+def test_batch_views_match_single_view_renders(bw):
+    import torch
+
+    bs, scenes, views, targets = _batch(bw)
+    bs.measure_capacity()
+    bs.step()
+    bs.check()
+    sums = [None] * len(scenes)
+    loss = 0.0
+    lengths = (bs.tile_bins[:, 1] - bs.tile_bins[:, 0]).long()
+    for k, v in enumerate(views):
+        s = _single(scenes[v["scene"]], v, targets[k], bw)
+        Ts, idx = bs.view_final(k)
+        torch.testing.assert_close(bs.view_image(k), s.img, rtol=0, atol=0)
+        torch.testing.assert_close(Ts, s.final_Ts, rtol=0, atol=0)
+        # final_idx indexes the batch's list: the view's own index plus the
+        # intersections of the views before it, for pixels with a contributor
+        off = int(lengths[:bs.views_host[k].tile_base].sum())
+        expect = torch.where(s.final_Ts < 1.0, s.final_idx + off, torch.zeros_like(s.final_idx))
+        torch.testing.assert_close(idx, expect, rtol=0, atol=0)
+        e = bs.view_entries(k)
+        for name, a, b in (("v_xy", bs.v_xy[e], s.v_xy), ("v_conic", bs.v_conic[e], s.v_conic)):
+            assert normwise_rel(a.cpu().numpy(), b.cpu().numpy()) <= 1e-5, (k, name)
+        g = {kk: vv.detach().cpu().numpy().astype(np.float64) for kk, vv in s.grads.items()}
+        sc = v["scene"]
+        sums[sc] = g if sums[sc] is None else {kk: sums[sc][kk] + g[kk] for kk in g}
+        loss += float(s.loss.item())
+    for sc in range(len(scenes)):
+        got = bs.scene_grads(sc)
+        for name in ("means3d", "scales", "quats", "colors", "opacities"):
+            assert normwise_rel(got[name].cpu().numpy(), sums[sc][name]) <= 1e-5, (sc, name)
+    assert abs(float(bs.loss.item()) - loss) <= 1e-5 * max(1.0, loss)
+
+
+def test_batch_graph_replay_matches_eager():
+    import torch
+
+    bs, *_ = _batch(16, (4000, 2500, 1000), 2)
+    bs.chunk = 3
+    bs.measure_capacity()
+    bs.step()
+    eager = bs.img.clone()
+    grads = {k: v.clone() for k, v in bs.scene_grads(0).items()}
+    count = bs.check()
+    bs.capture()
+    bs.replay()
+    bs.replay()
+    assert bs.check() == count
+    torch.testing.assert_close(bs.img, eager, rtol=0, atol=0)
+    for k, v in bs.scene_grads(0).items():
+        assert normwise_rel(v.cpu().numpy(), grads[k].cpu().numpy()) <= 1e-5, k
+
+
+def test_batch_capacity_overflow_is_reported():
+    from jaxsplat_gb300._lib import SplatError
+
+    bs, *_ = _batch(16)
+    bs._size(500)
+    bs.step()
+    with pytest.raises(SplatError, match="capacity-exceeded"):
+        bs.check()
+
+
+def test_batch_autotune_picks_a_measured_config():
+    bs, *_ = _batch(16, (2000, 3000), 2)
+    res = bs.autotune(block_sizes=(8, 16), chunks=(1, 4), steps=1)
+    assert set(res) == {(8, 1), (8, 4), (16, 1), (16, 4)}
+    assert bs.best == min(res, key=res.get)
+    assert bs.bw == bs.best[0] and bs.chunk == bs.best[1]
+    bs.replay()
+    bs.check()
