@@ -477,6 +477,45 @@ def add_stages_and_roofline(line, st, steps, flush):
 
 
 BATCH_METRIC = "batched fwd+bwd ms/iter, 4 scenes x 8 views"
+FIT_METRIC = "time to 30 dB PSNR, plain Adam from random init, 512x512 procedural, N=16384"
+
+
+def main_fit(a, torch, dev):
+    """--scene fit: wall-clock of the plain fitting loop (random init, Adam
+    lr 1e-2, one CUDA graph per step, PSNR checked every 25 steps) until the
+    render reaches 30 dB, on procedural 512x512 targets of held-out seeds."""
+    from jaxsplat_gb300.fit import Fitter
+    from jaxsplat_gb300.scenes import procedural_target
+
+    seeds = [10_000 + a.seed + k for k in range(max(1, a.steps))]
+    runs = []
+    for sd in seeds:
+        tgt = procedural_target(sd)
+        ft = Fitter(tgt, 16384, seed=sd, device=dev)
+        ft.run(3)  # warm-up: capture + first steps (untimed)
+        ft.check()
+        ft = Fitter(tgt, 16384, seed=sd, device=dev)
+        ft.capture()
+        torch.cuda.synchronize()
+        reached, steps, secs, psnr = ft.fit_until(30.0, max_steps=a.fit_max_steps, check_every=25)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        ft.run(20)
+        t1.record()
+        torch.cuda.synchronize()
+        runs.append({"seed": sd, "reached": reached, "steps": steps, "seconds": round(secs, 4),
+                     "psnr": round(psnr, 2), "ms_per_step": round(t0.elapsed_time(t1) / 20, 4)})
+    ok = [r["seconds"] for r in runs if r["reached"]]
+    value = round(float(np.mean(ok)), 4) if len(ok) == len(runs) else None
+    print(json.dumps({"metric": FIT_METRIC, "value": value, "unit": "s", "n_gpus": 1,
+                      "steps": len(runs), "warmup": 3, "higher_is_better": False,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                      "data": "synthetic (procedural targets, seeded)",
+                      "config": {"workload": "fit: 512x512 procedural target (64 blobs + 3 "
+                                             "gratings), 16384 Gaussians, random init, Adam lr 1e-2",
+                                 "max_steps": a.fit_max_steps, "check_every": 25},
+                      "runs": runs}))
 
 
 def main_batch(a, torch, world, rank, local, dist, dev):
@@ -556,6 +595,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-graph", action="store_true", help="eager launches instead of a CUDA graph")
+    ap.add_argument("--fit-max-steps", type=int, default=3000)
     ap.add_argument("--autotune", action="store_true",
                     help="batch scene: sweep block size x scheduler chunk before timing")
     a = ap.parse_args()
@@ -578,6 +618,8 @@ def main():
 
     if a.scene == "batch":
         return main_batch(a, torch, world, rank, local, dist, dev)
+    if a.scene == "fit":
+        return main_fit(a, torch, dev)
     sc = make_scene(a.scene, seed=a.seed)
     config = {"workload": f"{sc.spec.name}: {sc.spec.num_points} Gaussians, "
                           f"{sc.spec.img_shape[1]}x{sc.spec.img_shape[0]}, block 16, fp32, "

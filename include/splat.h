@@ -380,6 +380,42 @@ SPLAT_API int splat_batch_project_bwd(const splat_batch *b, const float *means3d
                                       float *v_scale, float *v_quat, splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* BF16 GEMM on the tensor cores (tcgen05, FP32 accumulation) for the
+ * warm-start network; no counterpart in the reference.
+ *   C[M,N] fp32 row-major (ldc) = A[M,K] x B[N,K]^T (+ C when accumulate),
+ *   A, B bf16 row-major (K contiguous; lda, ldb elements), 16-byte aligned,
+ *   K, lda, ldb multiples of 8.  status_dev (optional device uint32) gets
+ *   the look-back-timeout bit if a tensor-core wait runs out. */
+SPLAT_API int splat_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int lda,
+                              int ldb, int ldc, int accumulate, uint32_t *status_dev,
+                              splat_stream_t stream);
+
+/* Kernels around the GEMM for the warm-start network's 3x3 convolutions
+ * (padding 1, stride 1 or 2) on NHWC bf16 activations; no counterpart in the
+ * reference.
+ *   im2col3x3: x (n,h,w,c) bf16 -> cols (n*ho*wo, kpad) bf16, column
+ *     (ky*3 + kx)*c + ch, zeros past 9c (kpad >= 9c, a multiple of 8)
+ *   col2im3x3: dcols (n*ho*wo, kpad) fp32 -> dx (n,h,w,c) fp32 (overwritten)
+ *   bias_act:  y = act(acc + bias) (ReLU when relu != 0), rows x cols, to y
+ *     (bf16) and/or y32 (fp32)
+ *   act_grad:  dz = dy * [y > 0] (or dy) as bf16; dbias += column sums
+ *   transpose_bf16: out[c*ld_out + r] = in[r*cols + c]
+ *   adam: w -= lr mhat / (sqrt(vhat) + 1e-8) (b1 0.9, b2 0.999, step >= 1),
+ *     w16 (optional) = bf16(w) */
+SPLAT_API int splat_nn_im2col3x3(const void *x, void *cols, int n, int h, int w, int c, int stride,
+                                 int kpad, splat_stream_t stream);
+SPLAT_API int splat_nn_col2im3x3(const float *dcols, float *dx, int n, int h, int w, int c,
+                                 int stride, int kpad, splat_stream_t stream);
+SPLAT_API int splat_nn_bias_act(const float *acc, const float *bias, void *y, float *y32,
+                                int64_t rows, int cols, int relu, splat_stream_t stream);
+SPLAT_API int splat_nn_act_grad(const float *dy, const void *y, void *dz, float *dbias,
+                                int64_t rows, int cols, int relu, splat_stream_t stream);
+SPLAT_API int splat_nn_transpose_bf16(const void *in, void *out, int64_t rows, int cols,
+                                      int64_t ld_out, splat_stream_t stream);
+SPLAT_API int splat_nn_adam(float *w, float *m, float *v, const float *g, void *w16, int64_t n,
+                            float lr, int step, splat_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
 /* Self-test of the bounded wait: one block waits on a flag that nothing
  * sets, with `limit` polls, then records DEV_LOOKBACK_TIMEOUT in *status_dev
  * (device uint32) and returns.  Exists so the timeout path can be exercised

@@ -111,6 +111,13 @@ _SIGS = [
      + [C.c_uint32, _v, _v]),
     ("splat_batch_l2_loss", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 4 + [_v]),
     ("splat_batch_project_bwd", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 12 + [_v]),
+    ("splat_gemm_bf16", C.c_int, [_v, _v, _v] + [C.c_int] * 7 + [_v, _v]),
+    ("splat_nn_im2col3x3", C.c_int, [_v, _v] + [C.c_int] * 6 + [_v]),
+    ("splat_nn_col2im3x3", C.c_int, [_v, _v] + [C.c_int] * 6 + [_v]),
+    ("splat_nn_bias_act", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),
+    ("splat_nn_act_grad", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),
+    ("splat_nn_transpose_bf16", C.c_int, [_v, _v, C.c_int64, C.c_int, C.c_int64, _v]),
+    ("splat_nn_adam", C.c_int, [_v, _v, _v, _v, _v, C.c_int64, C.c_float, C.c_int, _v]),
 ]
 
 EXPORTED = [name for name, _, _ in _SIGS]

@@ -160,3 +160,32 @@ def make_batch(seed: int = 0, scene_points=BATCH_POINTS, views_per_scene: int = 
                               c=(w / 2.0, h / 2.0), background=np.zeros(3, np.float32)))
             targets.append(rng.uniform(0.0, 1.0, (h, w, 3)).astype(np.float32))
     return scenes, views, targets
+
+
+def procedural_target(seed: int, size: int = 512, blobs: int = 64, gratings: int = 3) -> np.ndarray:
+    """A (size, size, 3) fp32 image in [0, 1] drawn from a seed: a sum of
+    `blobs` random anisotropic 2D Gaussian blobs with random colours plus
+    `gratings` sinusoidal gratings (2-20 cycles across the image, random
+    orientation, phase and colour), rescaled into [0, 1]."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.meshgrid(np.arange(size, dtype=np.float64) + 0.5,
+                         np.arange(size, dtype=np.float64) + 0.5, indexing="ij")
+    img = np.zeros((size, size, 3))
+    for _ in range(blobs):
+        cx, cy = rng.uniform(0, size, 2)
+        sx, sy = np.exp(rng.uniform(np.log(size / 64), np.log(size / 6), 2))
+        th = rng.uniform(0, np.pi)
+        c, s = np.cos(th), np.sin(th)
+        dx, dy = xx - cx, yy - cy
+        u = (c * dx + s * dy) / sx
+        v = (-s * dx + c * dy) / sy
+        img += np.exp(-0.5 * (u * u + v * v))[..., None] * rng.uniform(0, 1, 3)
+    for _ in range(gratings):
+        cycles = rng.uniform(2, 20)
+        th = rng.uniform(0, np.pi)
+        phase = rng.uniform(0, 2 * np.pi)
+        w = 2 * np.pi * cycles / size
+        g = 0.5 + 0.5 * np.sin(w * (np.cos(th) * xx + np.sin(th) * yy) + phase)
+        img += g[..., None] * rng.uniform(0, 0.5, 3)
+    lo, hi = img.min(), img.max()
+    return ((img - lo) / max(hi - lo, 1e-12)).astype(np.float32)

@@ -1,0 +1,331 @@
+"""Learned warm start for single-image fitting.
+
+A small convolutional network looks at a 512x512 target image and proposes
+all 16384 Gaussians of the fit at once: an encoder of four 3x3 stride-2
+convolutions 3->32->64->128->256 (ReLU, BF16 activations and weights, FP32
+accumulation) down to a 32x32 grid, and a 1x1 convolution head emitting, per
+grid cell, 16 Gaussians x 14 raw parameters.  Every convolution runs as
+im2col + the tcgen05 BF16 GEMM of this library (gemm_tc.cu), forward and
+backward; the surrounding gathers, bias/ReLU and Adam are this library's
+kernels too (nn.cu).  torch only holds the buffers.
+
+Training data is what the plain fitting loop itself produces (``Fitter``
+from random init on procedural targets): each fitted set is put on the grid
+-- a Gaussian goes to the cell that contains its projected centre, a cell
+keeps its 16 most opaque Gaussians (empty slots are transparent
+placeholders) -- and the network regresses the standardised per-slot
+parameters (centre offset within the cell in cell units, depth, |scales|,
+sign-normalised unit quaternion, raw colours, raw opacity) with an MSE loss.
+
+Plain fitting from random init stays both the fallback and the judge: the
+measurement is wall-clock to 30 dB PSNR from the network's proposal versus
+from random init, on held-out seeds.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .fit import Fitter, camera, random_init
+
+GRID = 32           # cells per side
+SLOTS = 16          # Gaussians per cell
+NPARAM = 14         # raw parameters per Gaussian
+IMG = 512
+CELL = IMG // GRID  # pixels per cell side
+CHANNELS = (3, 32, 64, 128, 256)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _kpad(cin):
+    return (9 * cin + 7) // 8 * 8
+
+
+class ConvNet:
+    """The encoder + head with fp32 master weights, bf16 copies and Adam
+    state; forward/backward through libsplat's kernels on the current
+    stream."""
+
+    def __init__(self, device="cuda", seed: int = 0):
+        self.lib = _lib.load()
+        self.dev = torch.device(device)
+        g = torch.Generator().manual_seed(seed)
+        self.layers = []
+        for cin, cout in zip(CHANNELS[:-1], CHANNELS[1:]):
+            kp = _kpad(cin)
+            w = torch.zeros(cout, kp)
+            w[:, :9 * cin] = torch.randn(cout, 9 * cin, generator=g) * math.sqrt(2.0 / (9 * cin))
+            self.layers.append(self._param(w, torch.zeros(cout), cin, cout, kp))
+        wh = torch.randn(SLOTS * NPARAM, CHANNELS[-1], generator=g) * math.sqrt(1.0 / CHANNELS[-1])
+        self.head = self._param(wh, torch.zeros(SLOTS * NPARAM), CHANNELS[-1], SLOTS * NPARAM,
+                                CHANNELS[-1])
+        self.step_count = 0
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+
+    def _param(self, w, b, cin, cout, k):
+        d = self.dev
+        w = w.to(d).contiguous()
+        return dict(w=w, w16=w.to(torch.bfloat16).contiguous(), b=b.to(d).contiguous(),
+                    mw=torch.zeros_like(w), vw=torch.zeros_like(w), mb=torch.zeros_like(b.to(d)),
+                    vb=torch.zeros_like(b.to(d)), gw=torch.zeros_like(w),
+                    gb=torch.zeros_like(b.to(d)), cin=cin, cout=cout, k=k)
+
+    # -- primitives ------------------------------------------------------------
+    def _s(self):
+        return C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def gemm(self, A, B, Cm, M, N, K, lda, ldb, ldc, acc=False):
+        _lib.check(self.lib.splat_gemm_bf16(_p(A), _p(B), _p(Cm), M, N, K, lda, ldb, ldc, int(acc),
+                                            _p(self.status), self._s()), "gemm_bf16")
+
+    def transpose(self, x, rows, cols):
+        out = torch.empty(cols, rows, dtype=torch.bfloat16, device=self.dev)
+        _lib.check(self.lib.splat_nn_transpose_bf16(_p(x), _p(out), rows, cols, rows, self._s()),
+                   "transpose_bf16")
+        return out
+
+    # -- forward / backward ------------------------------------------------------
+    def forward(self, x):
+        """x: (B, 512, 512, 3) bf16 NHWC -> (B*32*32, 224) fp32."""
+        lib, s = self.lib, self._s()
+        B = x.shape[0]
+        h = x.shape[1]
+        self.saved = []
+        cur = x.contiguous()
+        for L in self.layers:
+            ho = (h - 1) // 2 + 1
+            P = B * ho * ho
+            cols = torch.empty(P, L["k"], dtype=torch.bfloat16, device=self.dev)
+            _lib.check(lib.splat_nn_im2col3x3(_p(cur), _p(cols), B, h, h, L["cin"], 2, L["k"], s),
+                       "im2col3x3")
+            acc = torch.empty(P, L["cout"], device=self.dev)
+            self.gemm(cols, L["w16"], acc, P, L["cout"], L["k"], L["k"], L["k"], L["cout"])
+            y = torch.empty(P, L["cout"], dtype=torch.bfloat16, device=self.dev)
+            _lib.check(lib.splat_nn_bias_act(_p(acc), _p(L["b"]), _p(y), None, P, L["cout"], 1, s),
+                       "bias_act")
+            self.saved.append((cols, y, h, ho, P))
+            cur, h = y, ho
+        Hd = self.head
+        P = cur.shape[0]
+        acc = torch.empty(P, Hd["cout"], device=self.dev)
+        self.gemm(cur, Hd["w16"], acc, P, Hd["cout"], Hd["k"], Hd["k"], Hd["k"], Hd["cout"])
+        out = torch.empty(P, Hd["cout"], device=self.dev)
+        _lib.check(lib.splat_nn_bias_act(_p(acc), _p(Hd["b"]), None, _p(out), P, Hd["cout"], 0, s),
+                   "bias_act")
+        self.head_in = cur
+        self.batch = B
+        return out
+
+    def backward(self, dout):
+        """dout: d(loss)/d(forward output), fp32; sets every parameter's
+        gradient."""
+        lib, s = self.lib, self._s()
+        B = self.batch
+        Hd = self.head
+        P = dout.shape[0]
+        for prm in self.layers + [Hd]:
+            prm["gw"].zero_()
+            prm["gb"].zero_()
+        dz = torch.empty(P, Hd["cout"], dtype=torch.bfloat16, device=self.dev)
+        _lib.check(lib.splat_nn_act_grad(_p(dout), None, _p(dz), _p(Hd["gb"]), P, Hd["cout"], 0, s),
+                   "act_grad")
+        # dWh = dz^T y4 ; dy4 = dz Wh
+        self.gemm(self.transpose(dz, P, Hd["cout"]), self.transpose(self.head_in, P, Hd["k"]),
+                  Hd["gw"], Hd["cout"], Hd["k"], P, P, P, Hd["k"])
+        dy = torch.empty(P, Hd["k"], device=self.dev)
+        self.gemm(dz, self.transpose(Hd["w16"], Hd["cout"], Hd["k"]), dy, P, Hd["k"], Hd["cout"],
+                  Hd["cout"], Hd["cout"], Hd["k"])
+        for i in range(len(self.layers) - 1, -1, -1):
+            L = self.layers[i]
+            cols, y, h, ho, P = self.saved[i]
+            dz = torch.empty(P, L["cout"], dtype=torch.bfloat16, device=self.dev)
+            _lib.check(lib.splat_nn_act_grad(_p(dy), _p(y), _p(dz), _p(L["gb"]), P, L["cout"], 1, s),
+                       "act_grad")
+            self.gemm(self.transpose(dz, P, L["cout"]), self.transpose(cols, P, L["k"]), L["gw"],
+                      L["cout"], L["k"], P, P, P, L["k"])
+            if i == 0:
+                break
+            dcols = torch.empty(P, L["k"], device=self.dev)
+            self.gemm(dz, self.transpose(L["w16"], L["cout"], L["k"]), dcols, P, L["k"], L["cout"],
+                      L["cout"], L["cout"], L["k"])
+            dy = torch.empty(B * h * h, L["cin"], device=self.dev)
+            _lib.check(lib.splat_nn_col2im3x3(_p(dcols), _p(dy), B, h, h, L["cin"], 2, L["k"], s),
+                       "col2im3x3")
+
+    def adam(self, lr: float):
+        self.step_count += 1
+        s = self._s()
+        for prm in self.layers + [self.head]:
+            _lib.check(self.lib.splat_nn_adam(_p(prm["w"]), _p(prm["mw"]), _p(prm["vw"]),
+                                              _p(prm["gw"]), _p(prm["w16"]), prm["w"].numel(), lr,
+                                              self.step_count, s), "adam")
+            _lib.check(self.lib.splat_nn_adam(_p(prm["b"]), _p(prm["mb"]), _p(prm["vb"]),
+                                              _p(prm["gb"]), None, prm["b"].numel(), lr,
+                                              self.step_count, s), "adam")
+
+    def check(self):
+        torch.cuda.synchronize(self.dev)
+        if int(self.status.item()):
+            raise _lib.SplatError("warm-start network: a tensor-core wait ran out")
+
+
+# ---------------------------------------------------------------------------
+# Fitted sets <-> the grid.
+
+def _cam():
+    cam = camera((IMG, IMG))
+    return cam["f"][0], cam["f"][1], cam["c"][0], cam["c"][1], float(cam["viewmat"][2, 3])
+
+
+def to_grid(params: dict) -> np.ndarray:
+    """A fitted set (raw parameters) -> (32*32, 16*14) per-slot parameters:
+    offset of the projected centre from the cell centre (cell units), depth
+    coordinate z, |scales|, sign-normalised unit quaternion, raw colours, raw
+    opacity (clipped to [-8, 8]); empty slots are transparent (opacity -8)."""
+    fx, fy, cx, cy, tz = _cam()
+    m = np.asarray(params["means3d"], np.float64)
+    zc = m[:, 2] + tz
+    px = fx * m[:, 0] / zc + cx
+    py = fy * m[:, 1] / zc + cy
+    gx = np.clip(np.floor(px / CELL), 0, GRID - 1).astype(np.int64)
+    gy = np.clip(np.floor(py / CELL), 0, GRID - 1).astype(np.int64)
+    q = np.asarray(params["quats"], np.float64)
+    q = q / np.maximum(np.linalg.norm(q, axis=1, keepdims=True), 1e-12)
+    q *= np.where(q[:, :1] < 0, -1.0, 1.0)
+    op = np.clip(np.asarray(params["opacities"], np.float64).reshape(-1), -8.0, 8.0)
+    feat = np.concatenate([
+        (px / CELL - gx - 0.5)[:, None], (py / CELL - gy - 0.5)[:, None], m[:, 2:3],
+        np.abs(np.asarray(params["scales"], np.float64)), q,
+        np.asarray(params["colors"], np.float64), op[:, None]], axis=1)
+    out = np.tile(empty_slot(), (GRID * GRID, SLOTS, 1))
+    cell = gy * GRID + gx
+    order = np.lexsort((-op, cell))  # by cell, most opaque first
+    cell_sorted = cell[order]
+    starts = np.searchsorted(cell_sorted, np.arange(GRID * GRID))
+    rank = np.arange(len(order)) - starts[cell_sorted]
+    keep = rank < SLOTS
+    out[cell_sorted[keep], rank[keep]] = feat[order[keep]]
+    return out.reshape(GRID * GRID, SLOTS * NPARAM).astype(np.float32)
+
+
+def empty_slot() -> np.ndarray:
+    return np.array([0, 0, 0, 0.02, 0.02, 0.02, 1, 0, 0, 0, 0, 0, 0, -8.0])
+
+
+def from_grid(grid: np.ndarray) -> dict:
+    """Inverse of to_grid: (32*32, 16*14) -> raw parameters of 16384
+    Gaussians (ready for ``Fitter(init=...)``)."""
+    fx, fy, cx, cy, tz = _cam()
+    g = np.asarray(grid, np.float64).reshape(GRID, GRID, SLOTS, NPARAM)
+    gy, gx = np.meshgrid(np.arange(GRID), np.arange(GRID), indexing="ij")
+    px = (gx[..., None] + 0.5 + g[..., 0]) * CELL
+    py = (gy[..., None] + 0.5 + g[..., 1]) * CELL
+    z = g[..., 2]
+    zc = z + tz
+    x = (px - cx) * zc / fx
+    y = (py - cy) * zc / fy
+    means = np.stack([x, y, z], -1).reshape(-1, 3)
+    flat = g.reshape(-1, NPARAM)
+    q = flat[:, 6:10]
+    q = q / np.maximum(np.linalg.norm(q, axis=1, keepdims=True), 1e-6)
+    return dict(means3d=means.astype(np.float32), scales=np.abs(flat[:, 3:6]).astype(np.float32),
+                quats=q.astype(np.float32), colors=flat[:, 10:13].astype(np.float32),
+                opacities=flat[:, 13:14].astype(np.float32))
+
+
+# ---------------------------------------------------------------------------
+# Data, training, evaluation.
+
+def fit_set(target: np.ndarray, seed: int, steps: int, device="cuda") -> dict:
+    """Plain fit (random init, Adam lr 1e-2) for `steps` steps -> raw params."""
+    ft = Fitter(target, SLOTS * GRID * GRID, seed=seed, device=device)
+    ft.run(steps)
+    ft.check()
+    return {k: v.detach().cpu().numpy() for k, v in ft.params().items()}
+
+
+class WarmStart:
+    """Trains the network on fitted sets and proposes initial parameters."""
+
+    def __init__(self, device="cuda", seed: int = 0):
+        self.dev = torch.device(device)
+        self.net = ConvNet(device, seed)
+        self.mu = np.zeros(SLOTS * NPARAM, np.float32)
+        self.sd = np.ones(SLOTS * NPARAM, np.float32)
+
+    def fit_normaliser(self, grids: np.ndarray):
+        per = grids.reshape(-1, SLOTS, NPARAM)
+        mu = per.mean(axis=(0, 1))
+        sd = per.std(axis=(0, 1)) + 1e-3
+        self.mu = np.tile(mu, SLOTS).astype(np.float32)
+        self.sd = np.tile(sd, SLOTS).astype(np.float32)
+
+    def _img(self, imgs):
+        return torch.as_tensor(np.asarray(imgs, np.float32)).to(self.dev).to(torch.bfloat16)
+
+    def train(self, images, grids, epochs: int = 20, batch: int = 8, lr: float = 1e-3,
+              log=None) -> list:
+        """images (S, 512, 512, 3), grids (S, 1024, 224) -> per-epoch mean loss."""
+        lib = _lib.load()
+        self.fit_normaliser(grids)
+        X = self._img(images)
+        Y = torch.as_tensor((np.asarray(grids) - self.mu) / self.sd).to(self.dev)
+        n = X.shape[0]
+        loss = torch.zeros(1, device=self.dev)
+        dout = torch.empty(batch * GRID * GRID, SLOTS * NPARAM, device=self.dev)
+        rng = np.random.default_rng(0)
+        hist = []
+        for ep in range(epochs):
+            perm = rng.permutation(n)
+            tot = 0.0
+            nb = n // batch
+            for b in range(nb):
+                idx = torch.as_tensor(perm[b * batch:(b + 1) * batch], device=self.dev)
+                out = self.net.forward(X[idx])
+                tgt = Y[idx].reshape(-1, SLOTS * NPARAM)
+                _lib.check(lib.splat_l2_loss(_p(out), _p(tgt), out.numel(), _p(loss), _p(dout),
+                                             C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)),
+                           "l2_loss")
+                self.net.backward(dout)
+                self.net.adam(lr)
+                tot += float(loss.item())
+            self.net.check()
+            hist.append(tot / max(nb, 1))
+            if log:
+                log(f"epoch {ep}: loss {hist[-1]:.4f}")
+        return hist
+
+    def propose(self, image) -> dict:
+        """Initial raw parameters of 16384 Gaussians for a target image."""
+        out = self.net.forward(self._img(np.asarray(image)[None]))
+        grid = out.cpu().numpy() * self.sd + self.mu
+        return from_grid(grid)
+
+
+def time_to_psnr(target, init=None, seed: int = 0, psnr: float = 30.0, max_steps: int = 3000,
+                 check_every: int = 25, device="cuda", propose=None):
+    """Wall-clock (s) to reach `psnr` dB: optional proposal (`propose(target)`),
+    then Fitter construction, graph capture and the fitting loop.  Returns
+    (reached, steps, seconds, final psnr)."""
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if propose is not None:
+        init = propose(target)
+    ft = Fitter(target, SLOTS * GRID * GRID, init=init, seed=seed, device=device)
+    ft.capture()
+    reached, steps, _, p = ft.fit_until(psnr, max_steps=max_steps, check_every=check_every)
+    torch.cuda.synchronize()
+    return reached, steps, time.perf_counter() - t0, p
+
+
+__all__ = ["ConvNet", "WarmStart", "to_grid", "from_grid", "fit_set", "time_to_psnr",
+           "random_init"]
