@@ -480,6 +480,31 @@ BATCH_METRIC = "batched fwd+bwd ms/iter, 4 scenes x 8 views"
 FIT_METRIC = "time to 30 dB PSNR, plain Adam from random init, 512x512 procedural, N=16384"
 
 
+WARM_METRIC = "time to 30 dB PSNR, learned init vs plain, 512x512 procedural, N=16384"
+
+
+def main_warmstart(a, torch, dev):
+    """--scene warmstart: dataset from the plain loop, network training, and
+    wall-clock to 30 dB from the network's proposal vs from random init on
+    held-out seeds (value = mean learned seconds; plain alongside)."""
+    from jaxsplat_gb300.warmstart import run_experiment
+
+    res = run_experiment(n_train=a.ws_train_sets, fit_steps=a.ws_fit_steps, epochs=a.ws_epochs,
+                         log=lambda m: print(m, file=sys.stderr), device=dev)
+    ev = res["eval"]
+    ok = all(r["learned_reached"] and r["plain_reached"] for r in ev)
+    learned = float(np.mean([r["learned_s"] for r in ev]))
+    plain = float(np.mean([r["plain_s"] for r in ev]))
+    print(json.dumps({"metric": WARM_METRIC, "value": round(learned, 4) if ok else None,
+                      "unit": "s", "plain_value": round(plain, 4) if ok else None,
+                      "n_gpus": 1, "steps": len(ev), "warmup": 1, "higher_is_better": False,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, f32 render",
+                      "data": "synthetic (procedural targets, seeded; training sets fitted here)",
+                      "config": {"workload": "warmstart: conv 3-32-64-128-256 + 1x1 head, 32x32x16 "
+                                             "Gaussians, 512x512 procedural targets"},
+                      "experiment": res}))
+
+
 def main_fit(a, torch, dev):
     """--scene fit: wall-clock of the plain fitting loop (random init, Adam
     lr 1e-2, one CUDA graph per step, PSNR checked every 25 steps) until the
@@ -596,6 +621,9 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-graph", action="store_true", help="eager launches instead of a CUDA graph")
     ap.add_argument("--fit-max-steps", type=int, default=3000)
+    ap.add_argument("--ws-train-sets", type=int, default=1000)
+    ap.add_argument("--ws-fit-steps", type=int, default=300)
+    ap.add_argument("--ws-epochs", type=int, default=20)
     ap.add_argument("--autotune", action="store_true",
                     help="batch scene: sweep block size x scheduler chunk before timing")
     a = ap.parse_args()
@@ -620,6 +648,8 @@ def main():
         return main_batch(a, torch, world, rank, local, dist, dev)
     if a.scene == "fit":
         return main_fit(a, torch, dev)
+    if a.scene == "warmstart":
+        return main_warmstart(a, torch, dev)
     sc = make_scene(a.scene, seed=a.seed)
     config = {"workload": f"{sc.spec.name}: {sc.spec.num_points} Gaussians, "
                           f"{sc.spec.img_shape[1]}x{sc.spec.img_shape[0]}, block 16, fp32, "

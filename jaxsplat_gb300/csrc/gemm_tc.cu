@@ -54,17 +54,20 @@ __host__ __device__ constexpr uint32_t mma_idesc(int m, int n) {
            ((uint32_t)(m >> 4) << 24);
 }
 
+// Polls (non-blocking test_wait) with a short sleep between polls; gives up
+// after `limit` polls (about limit x 0.1 us).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
     for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
             : "r"(bar), "r"(parity)
             : "memory");
         if (done) return true;
+        if (i > 64) __nanosleep(100);
     }
     return false;
 }
@@ -126,6 +129,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs 
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar1) : "memory");
+        // make the initialised barriers visible to the tensor cores' arrivals
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -263,7 +269,7 @@ int splat_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
     g.lda = lda; g.ldb = ldb; g.ldc = ldc;
     g.accumulate = accumulate;
     g.status = status_dev;
-    g.spin_limit = kDefaultSpinLimit;
+    g.spin_limit = 1u << 21;  // ~0.2 s of polling per wait
     // split K when the output has few tiles and K is long: partial sums of
     // `ktiles_per` K tiles each are added atomically into C (zeroed first
     // unless accumulating)

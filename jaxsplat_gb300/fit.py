@@ -86,6 +86,33 @@ class Fitter:
         self._transform()
         s.measure_capacity(self.headroom)
 
+    def reset(self, target=None, init: dict | None = None, seed: int = 0):
+        """Start a new fit in the same buffers (the captured graph stays
+        valid): a new target and/or new raw parameters (random if not
+        given), Adam state cleared."""
+        s = self.sess
+        if target is not None:
+            s.target.copy_(torch.as_tensor(np.asarray(target, np.float32)).reshape(s.target.shape))
+        if init is None:
+            init = random_init(self.n, seed)
+        s.means3d.copy_(torch.as_tensor(np.asarray(init["means3d"], np.float32)).reshape(self.n, 3))
+        s.scales.copy_(torch.as_tensor(np.asarray(init["scales"], np.float32)).reshape(self.n, 3))
+        self.quats_raw.copy_(torch.as_tensor(np.asarray(init["quats"], np.float32)).reshape(self.n, 4))
+        self.colors_raw.copy_(torch.as_tensor(np.asarray(init["colors"], np.float32)).reshape(self.n, 3))
+        self.opac_raw.copy_(torch.as_tensor(np.asarray(init["opacities"], np.float32)).reshape(self.n, 1))
+        self.m.zero_()
+        self.v.zero_()
+        self.step_count.zero_()
+        self.steps_done = 0
+        self._transform()
+        # the new parameters may hit more tiles: size the buffers for them
+        s._project()
+        torch.cuda.synchronize(s.dev)
+        count = int(s.total.item())
+        if count > 0.8 * s.capacity:
+            s._size(int(count * self.headroom) + 4096)
+            self.graph = None
+
     def _p(self, t):
         return C.c_void_p(t.data_ptr())
 
@@ -157,6 +184,14 @@ class Fitter:
         s = self.sess
         return dict(means3d=s.means3d, scales=s.scales, quats=self.quats_raw,
                     colors=self.colors_raw, opacities=self.opac_raw)
+
+    def check_render(self) -> float:
+        """PSNR of the current parameters' render (one eager step; the
+        parameters are not updated)."""
+        self._transform()
+        self.sess.step()
+        torch.cuda.synchronize(self.sess.dev)
+        return psnr(float(self.sess.loss.item()))
 
     def render(self):
         """The image of the current parameters."""

@@ -16,6 +16,7 @@ identity view matrix):
 
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -162,30 +163,64 @@ def make_batch(seed: int = 0, scene_points=BATCH_POINTS, views_per_scene: int = 
     return scenes, views, targets
 
 
-def procedural_target(seed: int, size: int = 512, blobs: int = 64, gratings: int = 3) -> np.ndarray:
-    """A (size, size, 3) fp32 image in [0, 1] drawn from a seed: a sum of
-    `blobs` random anisotropic 2D Gaussian blobs with random colours plus
-    `gratings` sinusoidal gratings (2-20 cycles across the image, random
-    orientation, phase and colour), rescaled into [0, 1]."""
+def _procedural_params(seed: int, size: int, blobs: int, gratings: int):
     rng = np.random.default_rng(seed)
-    yy, xx = np.meshgrid(np.arange(size, dtype=np.float64) + 0.5,
-                         np.arange(size, dtype=np.float64) + 0.5, indexing="ij")
-    img = np.zeros((size, size, 3))
+    bl = []
     for _ in range(blobs):
         cx, cy = rng.uniform(0, size, 2)
         sx, sy = np.exp(rng.uniform(np.log(size / 64), np.log(size / 6), 2))
         th = rng.uniform(0, np.pi)
-        c, s = np.cos(th), np.sin(th)
-        dx, dy = xx - cx, yy - cy
-        u = (c * dx + s * dy) / sx
-        v = (-s * dx + c * dy) / sy
-        img += np.exp(-0.5 * (u * u + v * v))[..., None] * rng.uniform(0, 1, 3)
+        bl.append((cx, cy, sx, sy, th, rng.uniform(0, 1, 3)))
+    gr = []
     for _ in range(gratings):
         cycles = rng.uniform(2, 20)
         th = rng.uniform(0, np.pi)
         phase = rng.uniform(0, 2 * np.pi)
+        gr.append((cycles, th, phase, rng.uniform(0, 0.5, 3)))
+    return bl, gr
+
+
+def procedural_target(seed: int, size: int = 512, blobs: int = 64, gratings: int = 3,
+                      device=None) -> np.ndarray:
+    """A (size, size, 3) fp32 image in [0, 1] drawn from a seed: a sum of
+    `blobs` random anisotropic 2D Gaussian blobs with random colours plus
+    `gratings` sinusoidal gratings (2-20 cycles across the image, random
+    orientation, phase and colour), rescaled into [0, 1].  With a torch
+    `device` the image is evaluated there in fp32 and returned as a tensor
+    (same draws; numpy evaluates in fp64)."""
+    bl, gr = _procedural_params(seed, size, blobs, gratings)
+    if device is not None:
+        import torch
+
+        ar = torch.arange(size, dtype=torch.float32, device=device) + 0.5
+        yy, xx = torch.meshgrid(ar, ar, indexing="ij")
+        img = torch.zeros(size, size, 3, device=device)
+        cos, sin = math.cos, math.sin
+    else:
+        yy, xx = np.meshgrid(np.arange(size, dtype=np.float64) + 0.5,
+                             np.arange(size, dtype=np.float64) + 0.5, indexing="ij")
+        img = np.zeros((size, size, 3))
+        cos, sin = np.cos, np.sin
+    lib = np if device is None else __import__("torch")
+    for cx, cy, sx, sy, th, col in bl:
+        c, s_ = cos(th), sin(th)
+        dx, dy = xx - cx, yy - cy
+        u = (c * dx + s_ * dy) / sx
+        v = (-s_ * dx + c * dy) / sy
+        img = img + lib.exp(-0.5 * (u * u + v * v))[..., None] * _as(col, img)
+    for cycles, th, phase, col in gr:
         w = 2 * np.pi * cycles / size
-        g = 0.5 + 0.5 * np.sin(w * (np.cos(th) * xx + np.sin(th) * yy) + phase)
-        img += g[..., None] * rng.uniform(0, 0.5, 3)
+        g = 0.5 + 0.5 * lib.sin(w * (cos(th) * xx + sin(th) * yy) + phase)
+        img = img + g[..., None] * _as(col, img)
     lo, hi = img.min(), img.max()
+    if device is not None:
+        return ((img - lo) / max(float(hi - lo), 1e-12)).float()
     return ((img - lo) / max(hi - lo, 1e-12)).astype(np.float32)
+
+
+def _as(col, like):
+    if isinstance(like, np.ndarray):
+        return col
+    import torch
+
+    return torch.as_tensor(np.asarray(col, np.float32), device=like.device)

@@ -281,7 +281,6 @@ class WarmStart:
         Y = torch.as_tensor((np.asarray(grids) - self.mu) / self.sd).to(self.dev)
         n = X.shape[0]
         loss = torch.zeros(1, device=self.dev)
-        dout = torch.empty(batch * GRID * GRID, SLOTS * NPARAM, device=self.dev)
         rng = np.random.default_rng(0)
         hist = []
         for ep in range(epochs):
@@ -291,6 +290,7 @@ class WarmStart:
             for b in range(nb):
                 idx = torch.as_tensor(perm[b * batch:(b + 1) * batch], device=self.dev)
                 out = self.net.forward(X[idx])
+                dout = torch.empty_like(out)
                 tgt = Y[idx].reshape(-1, SLOTS * NPARAM)
                 _lib.check(lib.splat_l2_loss(_p(out), _p(tgt), out.numel(), _p(loss), _p(dout),
                                              C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)),
@@ -311,21 +311,87 @@ class WarmStart:
         return from_grid(grid)
 
 
-def time_to_psnr(target, init=None, seed: int = 0, psnr: float = 30.0, max_steps: int = 3000,
-                 check_every: int = 25, device="cuda", propose=None):
-    """Wall-clock (s) to reach `psnr` dB: optional proposal (`propose(target)`),
-    then Fitter construction, graph capture and the fitting loop.  Returns
-    (reached, steps, seconds, final psnr)."""
+def time_to_psnr(fitter: Fitter, target, seed: int = 0, psnr: float = 30.0,
+                 max_steps: int = 3000, check_every: int = 5, propose=None):
+    """Wall-clock (s) for a reused, graph-captured Fitter to reach `psnr` dB
+    on `target`: the proposal (`propose(target)`, else random init from
+    `seed`), loading it, and the fitting loop.  Returns (reached, steps,
+    seconds, final psnr)."""
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    if propose is not None:
-        init = propose(target)
-    ft = Fitter(target, SLOTS * GRID * GRID, init=init, seed=seed, device=device)
-    ft.capture()
-    reached, steps, _, p = ft.fit_until(psnr, max_steps=max_steps, check_every=check_every)
+    init = propose(target) if propose is not None else None
+    fitter.reset(target, init=init, seed=seed)
+    reached, steps, _, p = fitter.fit_until(psnr, max_steps=max_steps, check_every=check_every)
     torch.cuda.synchronize()
     return reached, steps, time.perf_counter() - t0, p
 
 
 __all__ = ["ConvNet", "WarmStart", "to_grid", "from_grid", "fit_set", "time_to_psnr",
            "random_init"]
+
+
+def make_dataset(n_sets: int, fit_steps: int, first_seed: int = 0, device="cuda", log=None):
+    """Targets and grid-form fitted sets of `n_sets` procedural images
+    (seeds first_seed ..), each fitted by the plain loop for `fit_steps`
+    steps from random init.  One Fitter is reused (its graph stays valid)."""
+    from .scenes import procedural_target
+
+    imgs, grids = [], []
+    ft = None
+    for k in range(n_sets):
+        sd = first_seed + k
+        tgt = procedural_target(sd, IMG, device=device)
+        if ft is None:
+            ft = Fitter(tgt.cpu().numpy(), SLOTS * GRID * GRID, seed=sd, device=device)
+            ft.capture()
+        ft.reset(tgt, seed=sd)
+        ft.run(fit_steps)
+        ft.check()
+        if ft.graph is None:
+            ft.capture()
+        params = {kk: v.detach().cpu().numpy() for kk, v in ft.params().items()}
+        imgs.append(tgt.cpu().numpy())
+        grids.append(to_grid(params))
+        if log and (k + 1) % 100 == 0:
+            log(f"fitted {k + 1}/{n_sets}")
+    return np.stack(imgs), np.stack(grids)
+
+
+def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
+                   eval_seeds=tuple(range(1_000_000, 1_000_008)), psnr: float = 30.0,
+                   check_every: int = 5, device="cuda", log=None) -> dict:
+    """Dataset from the plain loop, training, then wall-clock to `psnr` dB on
+    held-out seeds from random init and from the network's proposal."""
+    from .scenes import procedural_target
+
+    t0 = time.perf_counter()
+    imgs, grids = make_dataset(n_train, fit_steps, device=device, log=log)
+    t_data = time.perf_counter() - t0
+    ws = WarmStart(device)
+    t1 = time.perf_counter()
+    hist = ws.train(imgs, grids, epochs=epochs, log=log)
+    t_train = time.perf_counter() - t1
+    rows = []
+    first = procedural_target(eval_seeds[0], IMG, device=device).cpu().numpy()
+    ft = Fitter(first, SLOTS * GRID * GRID, seed=0, device=device)
+    ft.capture()
+    # untimed warm-up of both paths (first-use costs)
+    time_to_psnr(ft, first, psnr=psnr, max_steps=20, check_every=check_every)
+    time_to_psnr(ft, first, psnr=psnr, max_steps=20, check_every=check_every, propose=ws.propose)
+    for sd in eval_seeds:
+        tgt = procedural_target(sd, IMG, device=device).cpu().numpy()
+        plain = time_to_psnr(ft, tgt, seed=sd, psnr=psnr, check_every=check_every)
+        learned = time_to_psnr(ft, tgt, seed=sd, psnr=psnr, check_every=check_every,
+                               propose=ws.propose)
+        ft.reset(tgt, init=ws.propose(tgt))
+        init_psnr = ft.check_render()
+        rows.append({"seed": int(sd), "plain_s": round(plain[2], 4), "plain_steps": plain[1],
+                     "plain_reached": bool(plain[0]), "learned_s": round(learned[2], 4),
+                     "learned_steps": learned[1], "learned_reached": bool(learned[0]),
+                     "learned_init_psnr": round(init_psnr, 2)})
+        if log:
+            log(str(rows[-1]))
+    return {"train_sets": n_train, "fit_steps": fit_steps, "epochs": epochs,
+            "data_s": round(t_data, 1), "train_s": round(t_train, 1),
+            "loss_first": round(hist[0], 4), "loss_last": round(hist[-1], 4), "eval": rows}
+

@@ -1,0 +1,66 @@
+"""The warm-start network's convolutions (im2col + tcgen05 GEMM, bias/ReLU,
+col2im) against torch's fp32 conv2d on the same bf16-rounded operands,
+forward and backward, and a short training run that lowers the loss."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float((a - b).abs().max() / max(1e-6, float(b.abs().max())))
+
+
+def test_conv_layer_forward_backward_match_torch():
+    import torch
+    import torch.nn.functional as F
+
+    from jaxsplat_gb300.warmstart import ConvNet
+
+    net = ConvNet("cuda", seed=1)
+    g = torch.Generator(device="cuda").manual_seed(2)
+    B, H = 2, 64
+    x = torch.rand(B, H, H, 3, device="cuda", generator=g).bfloat16()
+    out = net.forward(x)
+    # the same network in torch, fp32 on the bf16 weights
+    xt = x.float().permute(0, 3, 1, 2).requires_grad_(True)
+    h = xt
+    ws = []
+    for L in net.layers:
+        w = L["w16"].float()[:, :9 * L["cin"]].reshape(L["cout"], 3, 3, L["cin"]).permute(0, 3, 1, 2)
+        w = w.detach().requires_grad_(True)
+        b = L["b"].detach().clone().requires_grad_(True)
+        ws.append((w, b))
+        h = F.relu(F.conv2d(h, w, b, stride=2, padding=1))
+        h = h.bfloat16().float()  # the activations are stored as bf16
+    wh = net.head["w16"].float().detach().requires_grad_(True)
+    bh = net.head["b"].detach().clone().requires_grad_(True)
+    ref = (h.permute(0, 2, 3, 1).reshape(-1, h.shape[1]) @ wh.T) + bh
+    assert _rel(out, ref.detach()) < 2e-2
+    dout = torch.randn_like(out)
+    net.backward(dout)
+    (ref * dout).sum().backward()
+    assert _rel(net.head["gw"], wh.grad) < 3e-2
+    assert _rel(net.head["gb"], bh.grad) < 3e-2
+    for L, (w, b) in zip(net.layers, ws):
+        gw = L["gw"][:, :9 * L["cin"]].reshape(L["cout"], 3, 3, L["cin"]).permute(0, 3, 1, 2)
+        assert _rel(gw, w.grad) < 5e-2, L["cin"]
+        assert _rel(L["gb"], b.grad) < 5e-2, L["cin"]
+
+
+def test_training_lowers_the_loss():
+    import torch
+
+    from jaxsplat_gb300.warmstart import NPARAM, SLOTS, WarmStart
+
+    rng = np.random.default_rng(0)
+    imgs = rng.uniform(0, 1, (16, 64, 64, 3)).astype(np.float32)
+    # targets: a fixed linear function of 16x16 patch means, so they are learnable
+    patch = imgs.reshape(16, 4, 16, 4, 16, 3).mean(axis=(2, 4)).reshape(16, 16, 3)
+    proj = rng.normal(size=(3, SLOTS * NPARAM)).astype(np.float32)
+    grids = patch @ proj
+    ws = WarmStart("cuda", seed=0)
+    hist = ws.train(imgs, grids, epochs=30, batch=4, lr=3e-3)
+    torch.cuda.synchronize()
+    assert hist[-1] < 0.5 * hist[0], hist
