@@ -22,7 +22,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsplat.so")
 SOURCES = ["api.cu", "project.cu", "sort.cu", "raster.cu", "fit.cu", "noalloc.cu", "batch.cu", "gemm_tc.cu", "nn.cu"]
-HEADERS = ["splat_internal.cuh", "splat_math.cuh"]
+HEADERS = ["splat_internal.cuh", "splat_math.cuh", "project_math.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

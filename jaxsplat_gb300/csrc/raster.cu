@@ -512,7 +512,7 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
             float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             float g_op = 0.f, g_ax = 0.f, g_ay = 0.f;
             if (valid) {
-                const float ra = 1.f / (1.f - alpha);
+                const float ra = __frcp_rn(1.f - alpha);  // == 1.f / (1.f - alpha)
                 T *= ra;
                 const float fac = alpha * T;
                 g8[G_R] = fac * v_out.x;
@@ -724,7 +724,7 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
             for (int q = 0; q < 2; ++q) {
                 if (!valid[q]) continue;
                 BwdPixel &S = P[q];
-                const float ra = 1.f / (1.f - alpha[q]);
+                const float ra = __frcp_rn(1.f - alpha[q]);  // == 1.f / (1.f - alpha)
                 S.T *= ra;
                 const float fac = alpha[q] * S.T;
                 g8[G_R] += fac * S.v_out.x;

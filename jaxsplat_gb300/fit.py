@@ -92,7 +92,8 @@ class Fitter:
         given), Adam state cleared."""
         s = self.sess
         if target is not None:
-            s.target.copy_(torch.as_tensor(np.asarray(target, np.float32)).reshape(s.target.shape))
+            t = target if isinstance(target, torch.Tensor) else torch.as_tensor(np.asarray(target, np.float32))
+            s.target.copy_(t.reshape(s.target.shape))
         if init is None:
             init = random_init(self.n, seed)
         s.means3d.copy_(torch.as_tensor(np.asarray(init["means3d"], np.float32)).reshape(self.n, 3))
