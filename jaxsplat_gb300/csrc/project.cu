@@ -8,19 +8,21 @@
 // then writes cum_tiles_hit directly: one launch replaces the reference's
 // projection kernel + CUB scan + eight memsets + three host synchronisations
 // (lib/ops.cu:12-61).
+#include <algorithm>
+
 #include "project_math.cuh"
 #include "splat_internal.cuh"
 
 namespace splat {
 
-// A block of 512 threads projects a partition of 4096 Gaussians, eight
-// rounds of 512 consecutive ones: few partitions keep the look-back chain
-// short (its inclusive prefixes advance by one window of partitions per L2
-// round trip), and two blocks fit on an SM.
+// A block of 512 threads projects a partition of up to 4096 Gaussians, up
+// to eight rounds of 512 consecutive ones: few partitions keep the look-back
+// chain short (its inclusive prefixes advance by one window of partitions per
+// L2 round trip), and two blocks fit on an SM.  Small inputs take fewer
+// rounds per block so that every SM still gets work.
 constexpr int kProjThreads = 512;
-constexpr int kProjRounds = 8;
+constexpr int kProjRounds = 8;  // at most
 constexpr int kProjWarps = kProjThreads / 32;
-constexpr int kProjPart = kProjThreads * kProjRounds;
 
 struct ProjFwdArgs {
     int n;
@@ -33,6 +35,7 @@ struct ProjFwdArgs {
     unsigned long long *words;  // [0] ticket counter, [1 + b] look-back word of partition b
     uint32_t *status;
     uint32_t spin_limit;
+    int rounds;  // rounds of kProjThreads Gaussians per partition, 1..kProjRounds
 };
 
 // Inclusive scan over the block of one value per thread; returns the
@@ -76,11 +79,13 @@ __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a
 
     // forward.cu:37-116, every output written (the reference's memsets
     // provide the zeros of culled Gaussians); inclusive scan per round
+    const int part_size = a.rounds * kProjThreads;
     unsigned long long incl[kProjRounds];
     unsigned long long run = 0;
 #pragma unroll
     for (int r = 0; r < kProjRounds; ++r) {
-        const int i = part * kProjPart + r * kProjThreads + threadIdx.x;
+        if (r >= a.rounds) break;
+        const int i = part * part_size + r * kProjThreads + threadIdx.x;
         uint32_t hits = 0;
         if (i < a.n) {
             const ProjOut o = project_one(cam, a.means3d + 3 * (size_t)i, a.scales + 3 * (size_t)i,
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a
         }
         if (lane == 0) {
             s_prefix = excl;
-            const int nparts = (a.n + kProjPart - 1) / kProjPart;
+            const int nparts = (a.n + part_size - 1) / part_size;
             if (part == nparts - 1) {
                 const unsigned long long total = excl + run;
                 *a.total = (int64_t)total;
@@ -129,7 +134,8 @@ __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a
     const unsigned long long prefix = s_prefix;
 #pragma unroll
     for (int r = 0; r < kProjRounds; ++r) {
-        const int i = part * kProjPart + r * kProjThreads + threadIdx.x;
+        if (r >= a.rounds) break;
+        const int i = part * part_size + r * kProjThreads + threadIdx.x;
         // int32 wrap, as the reference's int32 scan
         if (i < a.n) a.cum[i] = (int32_t)(uint32_t)(prefix + incl[r]);
     }
@@ -180,7 +186,11 @@ int launch_project_fwd(const splat_params &p, const float *means3d, const float 
                        int32_t *ntiles, int32_t *cum, int64_t *total,
                        unsigned long long *words, cudaStream_t s) {
     const int n = (int)p.num_points;
-    const int nparts = (n + kProjPart - 1) / kProjPart;
+    // rounds per partition: as few as keep the partitions within one wave of
+    // two blocks per SM, at most 8
+    const int rounds = std::max(1, std::min(kProjRounds, (n + 2 * 152 * kProjThreads - 1) /
+                                                             (2 * 152 * kProjThreads)));
+    const int nparts = (n + rounds * kProjThreads - 1) / (rounds * kProjThreads);
     if (cudaMemsetAsync(words, 0, sizeof(unsigned long long) * (size_t)(nparts + 1), s) != cudaSuccess)
         return check_launch("project_fwd workspace memset");
     ProjFwdArgs a;
@@ -198,6 +208,7 @@ int launch_project_fwd(const splat_params &p, const float *means3d, const float 
     a.words = words;
     a.status = p.device_status;
     a.spin_limit = spin_limit(p);
+    a.rounds = rounds;
     project_fwd_kernel<<<nparts, kProjThreads, 0, s>>>(a);
     return check_launch("project_fwd_kernel");
 }

@@ -21,9 +21,9 @@
 //  * backward: the block starts at the largest final_idx of its pixels;
 //    per-Gaussian sums are reduced across the warp with a transposed butterfly
 //    (9 shuffles for 8 values) when many lanes contribute, or added per lane
-//    straight into shared memory when few do; the block's warps accumulate in
-//    shared memory and one global atomic per (tile, Gaussian, field) flushes
-//    them, instead of one per warp.
+//    when few do, and go to global memory with one atomic per field per
+//    (warp, Gaussian).  For 16x16 tiles a thread handles two pixels (see
+//    raster_bwd16_kernel).
 #include <math_constants.h>
 
 #include <algorithm>
@@ -385,7 +385,7 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-// Gradient fields accumulated per staged Gaussian.
+// Gradient fields of a (warp, Gaussian) pair.
 enum { G_R, G_G, G_B, G_CA, G_CB, G_CC, G_X, G_Y, G_OP, G_AX, G_AY, G_FIELDS };
 
 // With at most this many contributing lanes a warp adds per lane into shared
@@ -407,6 +407,14 @@ struct RasterBwdArgs {
     float *v_colors, *v_opac, *v_xy, *v_xy_abs, *v_conic;
 };
 
+// Global gradient slot of field f (G_R..G_Y) of list entry g whose colour
+// gradient goes to Gaussian gc.
+__device__ __forceinline__ float *grad_field(const RasterBwdArgs &a, int f, int g, int gc) {
+    return f < 3 ? a.v_colors + 3 * (size_t)gc + f
+         : f < 6 ? a.v_conic + 3 * (size_t)g + (f - 3)
+                 : a.v_xy + 2 * (size_t)g + (f - 6);
+}
+
 // kScene: the color and opacity gradients go to the Gaussian whose index the
 // record carries in r2.w (batched views of shared scenes) instead of the list
 // entry's own index.
@@ -419,8 +427,6 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
     __shared__ unsigned s_mask[kMaxTile];
     __shared__ int s_gid[kMaxTile];
     __shared__ int s_cidx[kScene ? kMaxTile : 1];
-    __shared__ float s_acc[kMaxTile][G_FIELDS];
-    __shared__ int s_touched[kMaxTile];
     __shared__ int s_wmax[kMaxWarps];
     __shared__ float4 s_rect[kMaxWarps];
     __shared__ uint8_t s_list[kMaxWarps][kMaxTile];
@@ -484,9 +490,6 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
                 s_mask[tr] = 0u;
             }
         }
-#pragma unroll
-        for (int f = 0; f < G_FIELDS; ++f) s_acc[tr][f] = 0.f;
-        s_touched[tr] = 0;
         __syncthreads();
         const int n = min(bsize, batch_end + 1 - range.x);
         const int cnt = warp_list(s_mask, max(0, batch_end - warp_bin_final), n, warp, lane, wmask,
@@ -534,46 +537,29 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
                     g_ay = fabsf(g8[G_Y]);
                 }
             }
-            if (lane == __ffs(vmask) - 1) s_touched[t] = 1;
+            // warp sums straight to global memory (see raster_bwd16_kernel)
+            const int g = s_gid[t];
+            const int gc = kScene ? s_cidx[t] : g;
             if (wmask == 0xffffffffu && __popc(vmask) > kFewLanes) {
                 const float s8 = warp_sum8_transposed(g8, lane);
                 const float sop = warp_sum(g_op);
-                if ((lane & 3) == 0) atomicAdd(&s_acc[t][lane >> 2], s8);
-                if (lane == 0) atomicAdd(&s_acc[t][G_OP], sop);
+                if ((lane & 3) == 0) atomicAdd(grad_field(a, lane >> 2, g, gc), s8);
+                if (lane == 0) atomicAdd(&a.v_opac[gc], sop);
                 if (kAbs) {
                     const float sax = warp_sum(g_ax), say = warp_sum(g_ay);
                     if (lane == 0) {
-                        atomicAdd(&s_acc[t][G_AX], sax);
-                        atomicAdd(&s_acc[t][G_AY], say);
+                        atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], sax);
+                        atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], say);
                     }
                 }
             } else if (valid) {
 #pragma unroll
-                for (int f = 0; f < 8; ++f) atomicAdd(&s_acc[t][f], g8[f]);
-                atomicAdd(&s_acc[t][G_OP], g_op);
+                for (int f = 0; f < 8; ++f) atomicAdd(grad_field(a, f, g, gc), g8[f]);
+                atomicAdd(&a.v_opac[gc], g_op);
                 if (kAbs) {
-                    atomicAdd(&s_acc[t][G_AX], g_ax);
-                    atomicAdd(&s_acc[t][G_AY], g_ay);
+                    atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], g_ax);
+                    atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], g_ay);
                 }
-            }
-        }
-        __syncthreads();
-        if (idx >= range.x && s_touched[tr]) {
-            const int g = s_gid[tr];
-            const int gc = kScene ? s_cidx[tr] : g;
-            const float *acc = s_acc[tr];
-            atomicAdd(&a.v_colors[3 * (size_t)gc + 0], acc[G_R]);
-            atomicAdd(&a.v_colors[3 * (size_t)gc + 1], acc[G_G]);
-            atomicAdd(&a.v_colors[3 * (size_t)gc + 2], acc[G_B]);
-            atomicAdd(&a.v_conic[3 * (size_t)g + 0], acc[G_CA]);
-            atomicAdd(&a.v_conic[3 * (size_t)g + 1], acc[G_CB]);
-            atomicAdd(&a.v_conic[3 * (size_t)g + 2], acc[G_CC]);
-            atomicAdd(&a.v_xy[2 * (size_t)g + 0], acc[G_X]);
-            atomicAdd(&a.v_xy[2 * (size_t)g + 1], acc[G_Y]);
-            atomicAdd(&a.v_opac[gc], acc[G_OP]);
-            if (kAbs) {
-                atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], acc[G_AX]);
-                atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], acc[G_AY]);
             }
         }
     }
@@ -591,7 +577,12 @@ __global__ void __launch_bounds__(kMaxTile) raster_bwd_kernel(RasterBwdArgs a) {
 // read from shared memory once per lane and evaluated for both pixels, and one
 // warp reduction covers 64 pixels.  Per-pixel arithmetic is unchanged.  (The
 // same layout in the forward measured slower than one pixel per thread, which
-// is what the forward keeps.)
+// is what the forward keeps.)  After the warp reduction the warp's sums go
+// straight to global memory, one atomic per field per (warp, Gaussian), as in
+// backward.cu:314-340: measured faster here than accumulating per (tile,
+// Gaussian) in shared memory and flushing after each batch (the global
+// reduction pipe is lightly loaded; the shared accumulators, their zeroing
+// and the flush barrier cost more).
 
 constexpr int kT16Threads = 128;
 constexpr int kT16Warps = 4;
@@ -624,8 +615,6 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
     __shared__ unsigned s_mask[kT16Batch];
     __shared__ int s_gid[kT16Batch];
     __shared__ int s_cidx[kScene ? kT16Batch : 1];
-    __shared__ float s_acc[kT16Batch][G_FIELDS];
-    __shared__ int s_touched[kT16Batch];
     __shared__ int s_wmax[kT16Warps];
     __shared__ float4 s_rect[kT16Warps];
     __shared__ uint8_t s_list[kT16Warps][kT16Batch];
@@ -686,9 +675,6 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
                     s_mask[e] = 0u;
                 }
             }
-#pragma unroll
-            for (int f = 0; f < G_FIELDS; ++f) s_acc[e][f] = 0.f;
-            s_touched[e] = 0;
         }
         __syncthreads();
         const int n = min(kT16Batch, batch_end + 1 - range.x);
@@ -748,48 +734,27 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
                     g_ay += fabsf(gy);
                 }
             }
-            if (lane == __ffs(vmask) - 1) s_touched[t] = 1;
+            const int g = s_gid[t];
+            const int gc = kScene ? s_cidx[t] : g;
             if (__popc(vmask) > kFewLanes) {
                 const float s8 = warp_sum8_transposed(g8, lane);
                 const float sop = warp_sum(g_op);
-                if ((lane & 3) == 0) atomicAdd(&s_acc[t][lane >> 2], s8);
-                if (lane == 0) atomicAdd(&s_acc[t][G_OP], sop);
+                if ((lane & 3) == 0) atomicAdd(grad_field(a, lane >> 2, g, gc), s8);
+                if (lane == 0) atomicAdd(&a.v_opac[gc], sop);
                 if (kAbs) {
                     const float sax = warp_sum(g_ax), say = warp_sum(g_ay);
                     if (lane == 0) {
-                        atomicAdd(&s_acc[t][G_AX], sax);
-                        atomicAdd(&s_acc[t][G_AY], say);
+                        atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], sax);
+                        atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], say);
                     }
                 }
             } else if (valid[0] || valid[1]) {
 #pragma unroll
-                for (int f = 0; f < 8; ++f) atomicAdd(&s_acc[t][f], g8[f]);
-                atomicAdd(&s_acc[t][G_OP], g_op);
+                for (int f = 0; f < 8; ++f) atomicAdd(grad_field(a, f, g, gc), g8[f]);
+                atomicAdd(&a.v_opac[gc], g_op);
                 if (kAbs) {
-                    atomicAdd(&s_acc[t][G_AX], g_ax);
-                    atomicAdd(&s_acc[t][G_AY], g_ay);
-                }
-            }
-        }
-        __syncthreads();
-        for (int e = tr; e < kT16Batch; e += kT16Threads) {
-            const int idx = batch_end - e;
-            if (idx >= range.x && s_touched[e]) {
-                const int g = s_gid[e];
-                const int gc = kScene ? s_cidx[e] : g;
-                const float *acc = s_acc[e];
-                atomicAdd(&a.v_colors[3 * (size_t)gc + 0], acc[G_R]);
-                atomicAdd(&a.v_colors[3 * (size_t)gc + 1], acc[G_G]);
-                atomicAdd(&a.v_colors[3 * (size_t)gc + 2], acc[G_B]);
-                atomicAdd(&a.v_conic[3 * (size_t)g + 0], acc[G_CA]);
-                atomicAdd(&a.v_conic[3 * (size_t)g + 1], acc[G_CB]);
-                atomicAdd(&a.v_conic[3 * (size_t)g + 2], acc[G_CC]);
-                atomicAdd(&a.v_xy[2 * (size_t)g + 0], acc[G_X]);
-                atomicAdd(&a.v_xy[2 * (size_t)g + 1], acc[G_Y]);
-                atomicAdd(&a.v_opac[gc], acc[G_OP]);
-                if (kAbs) {
-                    atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], acc[G_AX]);
-                    atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], acc[G_AY]);
+                    atomicAdd(&a.v_xy_abs[2 * (size_t)g + 0], g_ax);
+                    atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], g_ay);
                 }
             }
         }
