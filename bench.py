@@ -131,14 +131,21 @@ class OursStep:
                                   c=kw["c"], glob_scale=kw["glob_scale"],
                                   clip_thresh=kw["clip_thresh"], block_size=sc.spec.block_width,
                                   device=dev)
-        self.host = {k: torch.from_numpy(getattr(sc, k)).pin_memory()
-                     for k in ("means3d", "scales", "quats", "colors", "opacities", "viewmat",
-                               "background", "target")}
+        # inputs and outputs as single pinned blocks: one H2D and one D2H copy
+        # per step
+        self.host_in = self.sess.host_inputs(
+            *(getattr(sc, k) for k in ("means3d", "scales", "quats", "colors", "opacities",
+                                       "viewmat", "background", "target")))
+        self.host_out = torch.empty(self.sess.outputs.numel(), dtype=torch.float32,
+                                    pin_memory=True)
+        self.h2d_bytes = self.host_in.numel() * 4
+        self.d2h_bytes = self.host_out.numel() * 4
         self.upload()
         self.count = self.sess.measure_capacity()
         self.graph = graph
         if graph:
             self.sess.capture()
+            self.sess.capture_io(self.host_in, self.host_out)
         h, w = kw["img_shape"]
         bw = sc.spec.block_width
         tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
@@ -178,9 +185,18 @@ class OursStep:
                                 g["opacities"]]
 
     def upload(self):
-        h = self.host
-        self.sess.set_inputs(h["means3d"], h["scales"], h["quats"], h["colors"], h["opacities"],
-                             h["viewmat"], h["background"], h["target"])
+        self.sess.upload(self.host_in)
+
+    def download(self):
+        self.sess.download(self.host_out)
+
+    def step_e2e(self):
+        """Host input block to host output block with the copies overlapped
+        (RenderSession.step_io, as a graph)."""
+        if self.graph:
+            self.sess.replay_io()
+        else:
+            self.sess.step_io(self.host_in, self.host_out)
 
 
 class RefStep:
@@ -236,29 +252,30 @@ class BatchStep:
 
     STAGES = OursStep.STAGES
 
-    def __init__(self, seed, dev, graph=True, autotune=False, log=None):
+    def __init__(self, seed, dev, graph=True, autotune=False, log=None, points=None):
         import torch
 
         from jaxsplat_gb300.batch import BatchSession
-        from jaxsplat_gb300.scenes import make_batch
+        from jaxsplat_gb300.scenes import BATCH_POINTS, make_batch
 
         self.torch, self.dev = torch, dev
-        scenes, views, targets = make_batch(seed)
+        scenes, views, targets = make_batch(seed, scene_points=points or BATCH_POINTS)
         self.views = views
         self.sess = BatchSession(scenes, views, targets, block_size=16, chunk=1, device=dev)
         self.tuning = None
         if autotune:
             self.tuning = self.sess.autotune(log=log)
         s = self.sess
-        cat = lambda k, w: torch.from_numpy(np.concatenate(
-            [np.reshape(x[k], (-1, w)) for x in scenes]).astype(np.float32)).pin_memory()
-        self.host = {"means3d": cat("means3d", 3), "scales": cat("scales", 3),
-                     "quats": cat("quats", 4), "colors": cat("colors", 3),
-                     "opacities": cat("opacities", 1), "target": s.target.cpu().pin_memory()}
+        # the step's inputs and outputs as single pinned blocks (one copy each)
+        self.host_in = s.inputs.cpu().pin_memory()
+        self.host_out = torch.empty(s.outputs.numel(), dtype=torch.float32, pin_memory=True)
+        self.h2d_bytes = self.host_in.numel() * 4
+        self.d2h_bytes = self.host_out.numel() * 4
         self.count = s.measure_capacity()
         self.graph = graph
         if graph:
             s.capture()
+            s.capture_io(self.host_in, self.host_out)
         b = s.batch
         tile_passes = (max(1, (int(b.num_tiles) - 1).bit_length()) + 7) // 8
         # project, depth keys, 4-pass depth sort (+hist, offsets), emission
@@ -289,10 +306,18 @@ class BatchStep:
         return s.loss, [s.v_mean3d, s.v_scale, s.v_quat, s.v_colors, s.v_opacity]
 
     def upload(self):
-        s, h = self.sess, self.host
-        for dst, k in ((s.means3d, "means3d"), (s.scales, "scales"), (s.quats, "quats"),
-                       (s.colors, "colors"), (s.opacities, "opacities"), (s.target, "target")):
-            dst.copy_(h[k], non_blocking=True)
+        self.sess.upload(self.host_in)
+
+    def download(self):
+        self.sess.download(self.host_out)
+
+    def step_e2e(self):
+        """Host blocks in and out with the copies overlapped
+        (BatchSession.step_io, as a graph)."""
+        if self.graph:
+            self.sess.replay_io()
+        else:
+            self.sess.step_io(self.host_in, self.host_out)
 
 
 class RefBatchStep:
@@ -300,15 +325,15 @@ class RefBatchStep:
     jaxsplat user runs it: one render call per view, scene gradients summed
     over the views."""
 
-    def __init__(self, seed, dev):
+    def __init__(self, seed, dev, points=None):
         import torch
 
-        from jaxsplat_gb300.scenes import make_batch
+        from jaxsplat_gb300.scenes import BATCH_POINTS, make_batch
         from oracle.ref import RefKernels
 
         self.torch, self.dev = torch, dev
         self.rk = RefKernels()
-        scenes, views, targets = make_batch(seed)
+        scenes, views, targets = make_batch(seed, scene_points=points or BATCH_POINTS)
         self.views = views
         self.host = {}
         for i, x in enumerate(scenes):
@@ -397,24 +422,37 @@ def time_stages(st, steps, flush):
 
 
 def time_e2e(st, steps, flush):
-    """Host buffers: H2D of the inputs and D2H of loss + gradients inside."""
+    """Host buffers: H2D of the inputs and D2H of loss + gradients inside.
+    Steps with `download()` move their outputs as one block; the others copy
+    the loss and each gradient."""
     torch = st.torch
     out_host = None
     total = 0.0
-    bi = sum(v.numel() * v.element_size() for v in st.host.values())
-    bo = 0
+    bi = getattr(st, "h2d_bytes", None)
+    if bi is None:
+        bi = sum(v.numel() * v.element_size() for v in st.host.values())
+    bo = getattr(st, "d2h_bytes", 0)
     for _ in range(steps):
         flush.fill_(1)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
+        if hasattr(st, "step_e2e"):
+            st.step_e2e()
+            b.record()
+            torch.cuda.synchronize()
+            total += a.elapsed_time(b)
+            continue
         st.upload()
         loss, grads = st.step()
-        outs = [loss] + grads
-        if out_host is None:
-            out_host = [torch.empty(o.shape, dtype=o.dtype, pin_memory=True) for o in outs]
-            bo = sum(o.numel() * o.element_size() for o in outs)
-        for h, o in zip(out_host, outs):
-            h.copy_(o.reshape(h.shape), non_blocking=True)
+        if hasattr(st, "download"):
+            st.download()
+        else:
+            outs = [loss] + grads
+            if out_host is None:
+                out_host = [torch.empty(o.shape, dtype=o.dtype, pin_memory=True) for o in outs]
+                bo = sum(o.numel() * o.element_size() for o in outs)
+            for h, o in zip(out_host, outs):
+                h.copy_(o.reshape(h.shape), non_blocking=True)
         b.record()
         torch.cuda.synchronize()
         total += a.elapsed_time(b)
@@ -547,11 +585,12 @@ def main_batch(a, torch, world, rank, local, dist, dev):
     """--scene batch: the multi-scene, multi-view workload (one line)."""
     from jaxsplat_gb300.scenes import BATCH_POINTS, BATCH_SIZES
 
-    config = {"workload": "batch: 4 scenes (" + ", ".join(str(n) for n in BATCH_POINTS)
+    points = tuple(max(1, int(n * a.batch_scale)) for n in BATCH_POINTS)
+    config = {"workload": "batch: 4 scenes (" + ", ".join(str(n) for n in points)
                           + " Gaussians) x 8 views each, image sizes "
                           + "/".join(f"{w}x{h}" for h, w in BATCH_SIZES)
                           + " mixed, fp32, fwd+bwd with per-view L2 loss",
-              "scenes": list(BATCH_POINTS), "views_per_scene": 8,
+              "scenes": list(points), "views_per_scene": 8,
               "l2": "flushed before every timed step",
               "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
     if a.impl == "reference":
@@ -563,10 +602,10 @@ def main_batch(a, torch, world, rank, local, dist, dev):
             print(json.dumps({"impl": "reference", "unavailable":
                               "reference kernels (oracle/_ref) not built on this machine"}))
             return
-        st = RefBatchStep(a.seed, dev)
+        st = RefBatchStep(a.seed, dev, points)
     else:
         st = BatchStep(a.seed, dev, graph=not a.no_graph, autotune=a.autotune,
-                       log=lambda m: print(m, file=sys.stderr))
+                       log=lambda m: print(m, file=sys.stderr), points=points)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     if dist:
         dist.barrier()
@@ -621,6 +660,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-graph", action="store_true", help="eager launches instead of a CUDA graph")
     ap.add_argument("--fit-max-steps", type=int, default=3000)
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="batch scene: scale the scenes' Gaussian counts (profiling runs)")
     ap.add_argument("--ws-train-sets", type=int, default=1000)
     ap.add_argument("--ws-fit-steps", type=int, default=300)
     ap.add_argument("--ws-epochs", type=int, default=20)

@@ -28,8 +28,16 @@ from . import _lib
 from ._ops import _status_word
 
 
-def _f32(x, dev):
-    return torch.as_tensor(np.asarray(x, np.float32)).to(dev)
+def _block(shapes, device, pin=False):
+    """One fp32 buffer holding the named shapes back to back, each starting on
+    a 256-byte boundary; returns (buffer, {name: view})."""
+    offs, total = [], 0
+    for _, shape in shapes:
+        offs.append(total)
+        total += (math.prod(shape) + 63) // 64 * 64
+    buf = torch.zeros(total, dtype=torch.float32, device=device, pin_memory=pin)
+    return buf, {name: buf[o:o + math.prod(shape)].view(shape)
+                 for (name, shape), o in zip(shapes, offs)}
 
 
 class BatchSession:
@@ -50,16 +58,44 @@ class BatchSession:
         self.glob_scale, self.clip_thresh = float(glob_scale), float(clip_thresh)
         self.chunk = int(chunk)
         self.status = _status_word(self.dev)
-        dev = self.dev
-        cat = lambda k, w: _f32(np.concatenate([np.reshape(s[k], (-1, w)) for s in scenes]), dev)
-        self.means3d, self.scales, self.quats = cat("means3d", 3), cat("scales", 3), cat("quats", 4)
-        self.colors, self.opacities = cat("colors", 3), cat("opacities", 1)
+        G = sum(self.scene_points)
+        P = sum(int(v["img_shape"][0]) * int(v["img_shape"][1]) for v in self.view_specs)
+        # inputs (scene arrays, targets) and outputs (loss, scene gradients) as
+        # single blocks: one host transfer each way per step
+        self.inputs, views_in = _block(self.input_shapes(G, P), self.dev)
+        self.outputs, views_out = _block(self.output_shapes(G), self.dev)
+        for name, t in list(views_in.items()) + list(views_out.items()):
+            setattr(self, name, t)
+        for k, w in (("means3d", 3), ("scales", 3), ("quats", 4), ("colors", 3), ("opacities", 1)):
+            getattr(self, k).copy_(torch.as_tensor(np.concatenate(
+                [np.reshape(np.asarray(s[k], np.float32), (-1, w)) for s in scenes])))
+        self.target.zero_()
         self._targets = targets
         self._layout(int(block_size))
         if capacity is not None:
             self._size(int(capacity))
 
     # -- layout and buffers ----------------------------------------------------
+    @staticmethod
+    def input_shapes(G, P):
+        return [("means3d", (G, 3)), ("scales", (G, 3)), ("quats", (G, 4)), ("colors", (G, 3)),
+                ("opacities", (G, 1)), ("target", (P, 3))]
+
+    @staticmethod
+    def output_shapes(G):
+        # final after the rasterizer's backward first, then the projection's
+        return [("loss", (1,)), ("v_colors", (G, 3)), ("v_opacity", (G, 1)), ("v_mean3d", (G, 3)),
+                ("v_scale", (G, 3)), ("v_quat", (G, 4))]
+
+    def upload(self, host_block):
+        """All inputs of a step from a pinned host copy of ``self.inputs``."""
+        self.inputs.copy_(host_block, non_blocking=True)
+
+    def download(self, host_block):
+        """Loss and scene gradients into a pinned host block shaped like
+        ``self.outputs``."""
+        host_block.copy_(self.outputs, non_blocking=True)
+
     def _layout(self, block_size: int):
         n_views = len(self.view_specs)
         arr = (_lib.SplatView * n_views)()
@@ -99,15 +135,12 @@ class BatchSession:
         self.final_Ts, self.final_idx = Em(P, 1, **f32), Em(P, 1, **i32)
         self.img, self.v_img = Em(P, 3, **f32), Em(P, 3, **f32)
         self.v_alpha = torch.zeros(P, 1, **f32)
-        self.loss = Em(1, **f32)
-        self.target = torch.zeros(P, 3, **f32)
         if self._targets is not None:
             self.set_targets(self._targets)
-        self.v_colors, self.v_opacity = Em(G, 3, **f32), Em(G, 1, **f32)
         self.v_xy, self.v_conic = Em(E, 2, **f32), Em(E, 3, **f32)
-        self.v_mean3d, self.v_scale, self.v_quat = Em(G, 3, **f32), Em(G, 3, **f32), Em(G, 4, **f32)
         self.capacity = None
         self.graph = None
+        self.graph_io = None
 
     def _size(self, capacity: int):
         self.capacity = max(int(capacity), 1)
@@ -118,6 +151,7 @@ class BatchSession:
                                   self.lib.splat_last_error().decode())
         self.sort_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
         self.graph = None
+        self.graph_io = None
 
     def set_targets(self, targets):
         for k, t in enumerate(targets):
@@ -186,6 +220,53 @@ class BatchSession:
                                         P(self.v_mean3d), P(self.v_scale), P(self.v_quat), s),
             "batch_project_bwd")
         mark("end")
+
+    def step_io(self, host_in, host_out):
+        """One step from a pinned host copy of ``inputs`` to a pinned host
+        block the size of ``outputs``, the copies overlapped with the work:
+        the projection's inputs first, then colours, opacities and targets on
+        a second stream during the projection and sort; loss and colour /
+        opacity gradients back on the second stream during the projection
+        backward."""
+        if self.capacity is None:
+            self.measure_capacity()
+        cur = torch.cuda.current_stream(self.dev)
+        side = self._side = getattr(self, "_side", None) or torch.cuda.Stream(self.dev)
+        a_in = (self.colors.data_ptr() - self.inputs.data_ptr()) // 4
+        a_out = (self.v_mean3d.data_ptr() - self.outputs.data_ptr()) // 4
+        self.inputs[:a_in].copy_(host_in[:a_in], non_blocking=True)
+        side.wait_stream(cur)  # after the first half and the previous step
+        with torch.cuda.stream(side):
+            self.inputs[a_in:].copy_(host_in[a_in:], non_blocking=True)
+
+        def mark(name):
+            if name == "raster_fwd":
+                cur.wait_stream(side)
+            elif name == "project_bwd":
+                side.wait_stream(cur)
+                with torch.cuda.stream(side):
+                    host_out[:a_out].copy_(self.outputs[:a_out], non_blocking=True)
+
+        self.step(mark=mark)
+        host_out[a_out:].copy_(self.outputs[a_out:], non_blocking=True)
+        cur.wait_stream(side)
+
+    def capture_io(self, host_in, host_out):
+        if self.capacity is None:
+            self.measure_capacity()
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            self.step_io(host_in, host_out)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step_io(host_in, host_out)
+        self.graph_io = g
+        return g
+
+    def replay_io(self):
+        self.graph_io.replay()
 
     def capture(self):
         if self.capacity is None:

@@ -29,6 +29,18 @@ from . import _lib
 from ._ops import _status_word
 
 
+def _block(shapes, device, pin=False):
+    """One fp32 buffer holding the named shapes back to back, each starting on
+    a 256-byte boundary; returns (buffer, {name: view})."""
+    offs, total = [], 0
+    for _, shape in shapes:
+        offs.append(total)
+        total += (math.prod(shape) + 63) // 64 * 64
+    buf = torch.zeros(total, dtype=torch.float32, device=device, pin_memory=pin)
+    return buf, {name: buf[o:o + math.prod(shape)].view(shape)
+                 for (name, shape), o in zip(shapes, offs)}
+
+
 class RenderSession:
     def __init__(self, num_points: int, *, img_shape, f, c, glob_scale: float = 1.0,
                  clip_thresh: float = 0.01, block_size: int = 16, capacity: int | None = None,
@@ -46,11 +58,11 @@ class RenderSession:
         f32 = dict(dtype=torch.float32, device=self.dev)
         i32 = dict(dtype=torch.int32, device=self.dev)
         E = torch.empty
-        # inputs
-        self.means3d, self.scales = E(n, 3, **f32), E(n, 3, **f32)
-        self.quats, self.colors = E(n, 4, **f32), E(n, 3, **f32)
-        self.opacities, self.viewmat = E(n, 1, **f32), E(4, 4, **f32)
-        self.background, self.target = E(3, **f32), E(h, w, 3, **f32)
+        # inputs: views of one block, so that a host copy of the whole step's
+        # inputs is one transfer (see INPUTS / upload)
+        self.inputs, views = _block(self.input_shapes(), self.dev)
+        for name, t in views.items():
+            setattr(self, name, t)
         # projection
         self.cov3d, self.xys, self.depths = E(n, 6, **f32), E(n, 2, **f32), E(n, 1, **f32)
         self.radii, self.conics, self.comp = E(n, 1, **i32), E(n, 3, **f32), E(n, 1, **f32)
@@ -64,26 +76,61 @@ class RenderSession:
         self.packed = E(n, 12, **f32)
         self.final_Ts, self.final_idx = E(h, w, 1, **f32), E(h, w, 1, **i32)
         self.img = E(h, w, 3, **f32)
-        self.loss, self.v_img = E(1, **f32), E(h, w, 3, **f32)
+        self.v_img = E(h, w, 3, **f32)
         self.v_alpha = torch.zeros(h, w, 1, **f32)
-        # gradients
-        self.v_colors, self.v_opacity = E(n, 3, **f32), E(n, 1, **f32)
+        # loss and gradients: views of one block (one transfer to the host)
+        self.outputs, views = _block(self.output_shapes(), self.dev)
+        for name, t in views.items():
+            setattr(self, name, t)
         self.v_xy, self.v_conic = E(n, 2, **f32), E(n, 3, **f32)
         self.zeros_n1 = torch.zeros(n, 1, **f32)
-        self.v_mean3d, self.v_scale, self.v_quat = E(n, 3, **f32), E(n, 3, **f32), E(n, 4, **f32)
         self.v_cov2d, self.v_cov3d = E(n, 3, **f32), E(n, 6, **f32)
         self.capacity = None
         self.graph = None
+        self.graph_io = None
         if capacity is not None:
             self._size(int(capacity))
 
     # -- buffers -------------------------------------------------------------
+    def input_shapes(self):
+        n, h, w = self.n, self.h, self.w
+        # what the projection reads first, then what the rasterizer and the
+        # loss read (see step_io)
+        return [("means3d", (n, 3)), ("scales", (n, 3)), ("quats", (n, 4)), ("viewmat", (4, 4)),
+                ("colors", (n, 3)), ("opacities", (n, 1)), ("background", (3,)),
+                ("target", (h, w, 3))]
+
+    def output_shapes(self):
+        n = self.n
+        # what is final after the rasterizer's backward, then the projection's
+        return [("loss", (1,)), ("v_colors", (n, 3)), ("v_opacity", (n, 1)), ("v_mean3d", (n, 3)),
+                ("v_scale", (n, 3)), ("v_quat", (n, 4))]
+
+    def host_inputs(self, means3d, scales, quats, colors, opacities, viewmat, background, target):
+        """A pinned host block laid out like ``self.inputs`` (for ``upload``)."""
+        host, views = _block(self.input_shapes(), "cpu", pin=True)
+        src = dict(means3d=means3d, scales=scales, quats=quats, colors=colors,
+                   opacities=opacities, viewmat=viewmat, background=background, target=target)
+        for name, _ in self.input_shapes():
+            views[name].copy_(torch.as_tensor(src[name]).reshape(views[name].shape))
+        return host
+
+    def upload(self, host_block):
+        """All inputs of a step from a pinned host block (one transfer)."""
+        self.inputs.copy_(host_block, non_blocking=True)
+
+    def download(self, host_block):
+        """Loss and the five gradients into a pinned host block laid out like
+        ``self.outputs`` (one transfer)."""
+        host_block.copy_(self.outputs, non_blocking=True)
+
     def _size(self, capacity: int):
         self.capacity = max(int(capacity), 1)
         self.ids_sorted = torch.empty(self.capacity, dtype=torch.int32, device=self.dev)
         nbytes = self.lib.splat_sort_workspace_size(C.byref(self.params), self.capacity)
         self.sort_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
         self.graph = None
+        self.graph_io = None
 
     def set_inputs(self, means3d, scales, quats, colors, opacities, viewmat, background, target):
         for dst, src in ((self.means3d, means3d), (self.scales, scales), (self.quats, quats),
@@ -158,6 +205,61 @@ class RenderSession:
             P(self.v_conic), P(self.zeros_n1), P(self.v_mean3d), P(self.v_scale),
             P(self.v_quat), P(self.v_cov2d), P(self.v_cov3d), s), "project_bwd")
         mark("end")
+
+    def _split(self, buf, first):
+        """Offset in `buf` (a block) of the view named `first`."""
+        return (getattr(self, first).data_ptr() - buf.data_ptr()) // 4
+
+    def step_io(self, host_in, host_out):
+        """One step from a pinned host input block (``host_inputs``) to a
+        pinned host output block (the size of ``outputs``), with the copies
+        overlapped: the projection's inputs go first and the rest (colours,
+        opacities, background, target) on a second stream while the
+        projection and the sort run; loss and colour/opacity gradients go
+        back on the second stream while the projection backward runs."""
+        if self.capacity is None:
+            self.measure_capacity()
+        cur = torch.cuda.current_stream(self.dev)
+        side = self._side = getattr(self, "_side", None) or torch.cuda.Stream(self.dev)
+        a_in = self._split(self.inputs, "colors")
+        a_out = self._split(self.outputs, "v_mean3d")
+        self.inputs[:a_in].copy_(host_in[:a_in], non_blocking=True)
+        # the second half follows the first (copies in parallel would share the
+        # link and delay the projection) but overlaps the projection and sort;
+        # waiting on `cur` also orders it after the previous step's readers
+        side.wait_stream(cur)
+        with torch.cuda.stream(side):
+            self.inputs[a_in:].copy_(host_in[a_in:], non_blocking=True)
+        def mark(name):
+            if name == "raster_fwd":  # the rasterizer needs the second half
+                cur.wait_stream(side)
+            elif name == "project_bwd":  # colour/opacity gradients are final
+                side.wait_stream(cur)
+                with torch.cuda.stream(side):
+                    host_out[:a_out].copy_(self.outputs[:a_out], non_blocking=True)
+
+        self.step(mark=mark)
+        host_out[a_out:].copy_(self.outputs[a_out:], non_blocking=True)
+        cur.wait_stream(side)
+
+    def capture_io(self, host_in, host_out):
+        """Capture step_io(host_in, host_out) as a CUDA graph (after one eager
+        warm-up); replay with replay_io()."""
+        if self.capacity is None:
+            self.measure_capacity()
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            self.step_io(host_in, host_out)
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step_io(host_in, host_out)
+        self.graph_io = g
+        return g
+
+    def replay_io(self):
+        self.graph_io.replay()
 
     def capture(self):
         """Capture step() as a CUDA graph (after one eager warm-up step)."""

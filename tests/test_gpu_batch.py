@@ -112,3 +112,22 @@ def test_batch_autotune_picks_a_measured_config():
     assert bs.bw == bs.best[0] and bs.chunk == bs.best[1]
     bs.replay()
     bs.check()
+
+
+def test_batch_step_io_matches_device_step():
+    import torch
+
+    bs, *_ = _batch(16, (3000, 2000), 2)
+    bs.measure_capacity()
+    host_in = bs.inputs.cpu().pin_memory()
+    host_out = torch.empty(bs.outputs.numel(), dtype=torch.float32, pin_memory=True)
+    bs.capture_io(host_in, host_out)
+    host_out.fill_(float("nan"))
+    bs.replay_io()
+    torch.cuda.synchronize()
+    got = host_out.clone()
+    bs.step()
+    torch.cuda.synchronize()
+    ref = bs.outputs.cpu()
+    assert abs(float(got[0]) - float(ref[0])) <= 1e-6 * max(1.0, abs(float(ref[0])))
+    assert normwise_rel(got.numpy(), ref.numpy()) <= 1e-5

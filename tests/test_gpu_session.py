@@ -89,3 +89,29 @@ def test_capacity_overflow_is_reported():
     sess.step()
     with pytest.raises(SplatError, match="capacity-exceeded"):
         sess.check()
+
+
+def test_step_io_copies_inputs_in_and_results_out():
+    """step_io / its graph: the host input block reaches the device (a changed
+    target changes the loss), and the host output block holds the same loss
+    and gradients as a device step on those inputs."""
+    import torch
+
+    sc = _scene()
+    sess = _session(sc)
+    sess.measure_capacity()
+    target_b = (sc.target * 0.5 + 0.25).astype(np.float32)
+    host_in = sess.host_inputs(sc.means3d, sc.scales, sc.quats, sc.colors, sc.opacities,
+                               sc.viewmat, sc.background, target_b)
+    host_out = torch.empty(sess.outputs.numel(), dtype=torch.float32, pin_memory=True)
+    sess.capture_io(host_in, host_out)
+    host_out.fill_(float("nan"))
+    sess.replay_io()
+    torch.cuda.synchronize()
+    got = host_out.clone()
+    sess.step()  # same (uploaded) inputs, device only
+    torch.cuda.synchronize()
+    ref = sess.outputs.cpu()
+    assert abs(float(got[0]) - float(ref[0])) <= 1e-6 * max(1.0, abs(float(ref[0])))
+    assert normwise_rel(got.numpy(), ref.numpy()) <= 1e-5
+    torch.testing.assert_close(sess.target.cpu(), torch.from_numpy(target_b), rtol=0, atol=0)
