@@ -47,16 +47,26 @@ __device__ __forceinline__ ProjCam view_cam(const splat_view &v, float glob, flo
 
 __global__ void __launch_bounds__(kBatchBlock) batch_project_fwd_kernel(BatchProjArgs a) {
     __shared__ unsigned s_hits[kBatchBlock / 32];
+    __shared__ ProjCam s_cam;
+    __shared__ uint32_t s_base, s_gbase, s_npts;
     const size_t i = (size_t)blockIdx.x * kBatchBlock + threadIdx.x;
-    const splat_view &v = a.views[view_by_entry(a.views, a.nviews, (uint32_t)(i - threadIdx.x))];
-    const uint32_t k = (uint32_t)(i - v.entry_base);
+    if (threadIdx.x == 0) {
+        // the block's view (blocks never straddle views); its camera once per
+        // block -- the tangents are evaluated in double, slow on this GPU
+        const splat_view &v = a.views[view_by_entry(a.views, a.nviews, (uint32_t)i)];
+        s_cam = view_cam(v, a.glob_scale, a.clip, a.bw);
+        s_base = v.entry_base;
+        s_gbase = v.gauss_base;
+        s_npts = v.num_points;
+    }
+    __syncthreads();
+    const uint32_t k = (uint32_t)(i - s_base);
     uint32_t hits = 0;
     if (i < a.entries) {
         ProjOut o;
-        if (k < v.num_points) {
-            const size_t g = (size_t)v.gauss_base + k;
-            o = project_one(view_cam(v, a.glob_scale, a.clip, a.bw), a.means3d + 3 * g,
-                            a.scales + 3 * g, a.quats + 4 * g);
+        if (k < s_npts) {
+            const size_t g = (size_t)s_gbase + k;
+            o = project_one(s_cam, a.means3d + 3 * g, a.scales + 3 * g, a.quats + 4 * g);
         } else {  // padding: a culled Gaussian
 #pragma unroll
             for (int q = 0; q < 6; ++q) o.cov[q] = 0.f;
