@@ -45,6 +45,9 @@ L2_FLUSH_BYTES = 256 << 20
 # the dominant kernel on the 1M-Gaussian 1920x1080 scene, from the ncu capture
 # summarised in profiles/raster_bwd16_hd.md (104.17 MB read + 4.87 MB written).
 NCU_TRAFFIC = {"raster_bwd": 104_166_400 + 4_871_168}
+# The batched backward captured at a quarter of the batch's Gaussian counts
+# (profiles/kernels_batch_quarter.md): bytes read, bytes written, intersections.
+NCU_BATCH_QUARTER = {"raster_bwd": (1_278_222_080, 106_604_800, 23_673_320)}
 
 
 def _peaks():
@@ -173,6 +176,12 @@ class OursStep:
                 "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes,
                 "project_fwd": 100 * n, "project_bwd": 140 * n, "l2_loss": 36 * P}
 
+    def ncu_traffic(self, kernel):
+        """Measured DRAM bytes of one launch (ncu), for the 1080p scene only."""
+        if self.sc.spec.name != "hd" or kernel not in NCU_TRAFFIC:
+            return None, None
+        return NCU_TRAFFIC[kernel], "ncu capture of this workload"
+
     def step(self, ev=None):
         if ev is not None:
             self.sess.step(mark=lambda name: ev[name].record())
@@ -294,6 +303,18 @@ class BatchStep:
         return {"raster_bwd": 76 * I + 24 * P, "raster_fwd": 40 * I + 20 * P + 84 * E,
                 "sort": 16 * E * 4 + 28 * E + 8 * I + 16 * I * self.passes,
                 "project_fwd": 100 * E, "project_bwd": 140 * E, "l2_loss": 36 * P}
+
+    def ncu_traffic(self, kernel):
+        """DRAM bytes of one launch scaled from the quarter-size capture: the
+        per-pixel reads (final_Ts, final_idx, v_img, v_img_alpha: 24 B per
+        pixel, the same pixels at every scale) stay, the rest (records,
+        lists, gradient writes) scales with the intersections."""
+        if kernel not in NCU_BATCH_QUARTER:
+            return None, None
+        rd, wr, iq = NCU_BATCH_QUARTER[kernel]
+        pix = 24 * int(self.sess.batch.num_pixels)
+        est = pix + (rd + wr - pix) * self.count / iq
+        return int(est), "quarter-size ncu capture, non-pixel bytes scaled by intersections"
 
     def step(self, ev=None):
         if ev is not None:
@@ -511,10 +532,13 @@ def add_stages_and_roofline(line, st, steps, flush):
     bytes_by_stage = st.stage_bytes()
     peak, src = _peaks()
     achieved = bytes_by_stage[dominant] / (stage_ms[dominant] * 1e-3) / 1e9
+    traffic, traffic_src = st.ncu_traffic(dominant)
     line["roofline"] = {"kernel": dominant, "bound": "hbm", "achieved": round(achieved, 1),
                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                        "peak_source": src, "traffic": NCU_TRAFFIC.get(dominant),
+                        "peak_source": src, "traffic": traffic,
                         "algorithmic_bytes": bytes_by_stage[dominant]}
+    if traffic is not None:
+        line["roofline"]["traffic_source"] = traffic_src
 
 
 BATCH_METRIC = "batched fwd+bwd ms/iter, 4 scenes x 8 views"
