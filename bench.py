@@ -163,16 +163,16 @@ class OursStep:
         return self.kernels_per_step
 
     def stage_bytes(self):
-        """Algorithmic bytes per stage: raster backward gathers 40 B per
-        intersection (4 B id + the 36 B of xy, conic, opacity and color it
-        uses), issues 9 fp32 atomics (36 B) per (tile, Gaussian) pair, and
-        reads 24 B per pixel (final_Ts, final_idx, v_img, v_img_alpha); the
-        forward stage adds the packing pass (36 B in + 48 B out per
-        Gaussian)."""
+        """Algorithmic bytes per stage.  Raster backward: 52 B per
+        intersection, 32 B per pixel and 9 fp32 atomics (36 B) per
+        contributing (tile, Gaussian) pair I_c, counted by splat_count_pairs
+        (`pairs`, when taken); raster forward: 40 B per intersection and 20 B
+        per pixel, plus the packing pass (36 B in + 48 B out per Gaussian)."""
         n, I = self.sc.spec.num_points, self.count
         h, w = self.sc.spec.img_shape
         P = h * w
-        return {"raster_bwd": 76 * I + 24 * P, "raster_fwd": 40 * I + 20 * P + 84 * n,
+        ic = (getattr(self, "pairs", None) or {}).get("tile_gaussian_contributing", 0)
+        return {"raster_bwd": 52 * I + 32 * P + 36 * ic, "raster_fwd": 40 * I + 20 * P + 84 * n,
                 "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes,
                 "project_fwd": 100 * n, "project_bwd": 140 * n, "l2_loss": 36 * P}
 
@@ -297,10 +297,11 @@ class BatchStep:
         return self.kernels_per_step
 
     def stage_bytes(self):
-        """As OursStep.stage_bytes over E (view, Gaussian) entries."""
+        """As OursStep.stage_bytes over E (view, Gaussian) entries, without the
+        atomics term (no pair count for batches: a lower bound)."""
         b, I = self.sess.batch, self.count
         E, P = int(b.num_entries), int(b.num_pixels)
-        return {"raster_bwd": 76 * I + 24 * P, "raster_fwd": 40 * I + 20 * P + 84 * E,
+        return {"raster_bwd": 52 * I + 32 * P, "raster_fwd": 40 * I + 20 * P + 84 * E,
                 "sort": 16 * E * 4 + 28 * E + 8 * I + 16 * I * self.passes,
                 "project_fwd": 100 * E, "project_bwd": 140 * E, "l2_loss": 36 * P}
 
@@ -539,6 +540,61 @@ def add_stages_and_roofline(line, st, steps, flush):
                         "algorithmic_bytes": bytes_by_stage[dominant]}
     if traffic is not None:
         line["roofline"]["traffic_source"] = traffic_src
+
+
+# Nominal per-SM rates of sm_103a: 128 FP32 lanes (an FMA counts as 2
+# FLOPs) and 16 MUFU ex2 results per clock.  Scaled by the SM count and the SM
+# clock sampled during the run.
+FP32_FLOPS_PER_SM_CLK = 256
+EX2_PER_SM_CLK = 16
+# FP32 operations per evaluated pixel-Gaussian pair (falloff, exponent,
+# alpha, blend) and the further ones per contributing pair in the backward
+# (transmittance, colour, alpha, conic and position cotangents).
+FLOPS_PER_EVAL = 15
+FLOPS_PER_CONTRIB_BWD = 30
+
+
+def add_compute_roofline(line, st):
+    """Per-stage floors from the step's own work counts: HBM bytes over the
+    measured copy bandwidth for every stage; for the rasterizers also FP32
+    FLOPs and ex2 counts over the nominal rates (from splat_count_pairs).
+    `step.frac` = the sum of the stage floors over the measured step time."""
+    import torch
+
+    pairs = st.pairs
+    line["pairs"] = pairs
+    peak, src = _peaks()
+    props = torch.cuda.get_device_properties(st.dev)
+    clk = (line.get("clocks") or {}).get("sm_mhz") or (line.get("clocks") or {}).get("sm_max_mhz")
+    if not clk:
+        return
+    sms = props.multi_processor_count
+    fp32 = sms * FP32_FLOPS_PER_SM_CLK * clk * 1e6
+    ex2 = sms * EX2_PER_SM_CLK * clk * 1e6
+    work = st.stage_bytes()
+    flops = {"raster_fwd": FLOPS_PER_EVAL * pairs["fwd_evaluated"],
+             "raster_bwd": FLOPS_PER_EVAL * pairs["bwd_evaluated"]
+             + FLOPS_PER_CONTRIB_BWD * pairs["bwd_contributing"]}
+    sfu = {"raster_fwd": pairs["fwd_evaluated"], "raster_bwd": pairs["bwd_evaluated"]}
+    stages, total_floor = {}, 0.0
+    for name, ms in line["stages_ms"].items():
+        if name not in work:
+            continue
+        floors = {"hbm": work[name] / (peak * 1e9) * 1e3}
+        if name in flops:
+            floors["fp32"] = flops[name] / fp32 * 1e3
+            floors["sfu"] = sfu[name] / ex2 * 1e3
+        bound = max(floors, key=floors.get)
+        total_floor += floors[bound]
+        stages[name] = {"ms": ms, "floor_ms": round(floors[bound], 4), "bound": bound,
+                        "frac": round(floors[bound] / ms, 4)}
+    line["stage_roofline"] = {
+        "stages": stages,
+        "step": {"floor_ms": round(total_floor, 4), "ms": line["value"],
+                 "frac": round(total_floor / line["value"], 4)},
+        "peaks": {"hbm_gbs": peak, "hbm_source": src,
+                  "fp32_tflops": round(fp32 / 1e12, 1), "ex2_per_s": ex2,
+                  "compute_source": f"nominal per-SM rates x {sms} SMs x {clk:.0f} MHz"}}
 
 
 BATCH_METRIC = "batched fwd+bwd ms/iter, 4 scenes x 8 views"
@@ -780,7 +836,9 @@ def main():
         st.sess.check()  # no step overflowed its capacity, no device check fired
         line["gpu_launches"] = st.launches_per_step() * a.steps
         line["cuda_graph"] = st.graph
+        st.pairs = st.sess.count_pairs()  # work counts of the timed step's list
         add_stages_and_roofline(line, st, a.steps, flush)
+        add_compute_roofline(line, st)
         if not a.no_cpu_baseline and world == 1:
             line["cpu_baseline"] = cpu_baseline(sc)
     print(json.dumps(line))

@@ -186,6 +186,24 @@ SPLAT_API int splat_project_bwd(const splat_params *p, const float *means3d, con
                       const float *v_compensation, float *v_mean3d, float *v_scale,
                       float *v_quat, float *v_cov2d, float *v_cov3d, splat_stream_t stream);
 
+/* Work counts of one forward+backward over a sorted list, for a compute
+ * roofline (diagnostic, no reference counterpart; one block per tile, not
+ * on the step path).  Same list arguments as splat_rasterize_fwd plus the
+ * forward's final_idx.  counts (device, 4 x uint64, overwritten):
+ *   [0] pixel-Gaussian pairs the reference's forward evaluates (per pixel,
+ *       list entries up to and including the saturating one,
+ *       lib/kernels/forward.cu:380-455);
+ *   [1] pairs its backward evaluates (entries up to final_idx,
+ *       lib/kernels/backward.cu:240-262);
+ *   [2] of those, the contributing pairs (sigma >= 0, alpha >= 1/255);
+ *   [3] (tile, Gaussian) pairs with a contributing pixel (the granularity of
+ *       the backward's gradient atomics, lib/kernels/backward.cu:314-340). */
+SPLAT_API int splat_count_pairs(const splat_params *p, int64_t num_intersects,
+                                const int64_t *count_dev, const int32_t *gaussian_ids_sorted,
+                                const int32_t *tile_bins, const float *packed,
+                                const int32_t *final_idx, uint64_t *counts,
+                                splat_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Mean squared error against a target and its cotangent:
  * loss_out[0] = mean((img - target)^2), v_img = 2 (img - target) / count.

@@ -87,6 +87,7 @@ _SIGS = [
     ("splat_rasterize_bwd", C.c_int, [_P, C.c_int64] + [_v] * 14 + [_v]),
     ("splat_project_bwd", C.c_int, [_P] + [_v] * 17 + [_v]),
     ("splat_l2_loss", C.c_int, [_v, _v, C.c_int64, _v, _v, _v]),
+    ("splat_count_pairs", C.c_int, [_P, C.c_int64] + [_v] * 6 + [_v]),
     ("splat_xla_project_fwd", None, [_v, C.POINTER(_v), C.c_char_p, C.c_size_t]),
     ("splat_xla_project_bwd", None, [_v, C.POINTER(_v), C.c_char_p, C.c_size_t]),
     ("splat_xla_rasterize_fwd", None, [_v, C.POINTER(_v), C.c_char_p, C.c_size_t]),

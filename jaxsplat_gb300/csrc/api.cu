@@ -28,6 +28,8 @@ int launch_raster_bwd(const splat_params &, Count, const int32_t *, const int2 *
                       const float *, const float *, const float *, const int32_t *,
                       const float *, const float *, float *, float *, float *, float *, float *,
                       cudaStream_t);
+int launch_count_pairs(const splat_params &, Count, const int32_t *, const int2 *, const float *,
+                       const int32_t *, unsigned long long *, cudaStream_t);
 
 static thread_local std::string g_error;
 
@@ -318,6 +320,24 @@ int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int
     return launch_raster_fwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
                              final_Ts, final_idx, out_img, (cudaStream_t)stream);
+}
+
+int splat_count_pairs(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
+                      const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                      const float *packed, const int32_t *final_idx, uint64_t *counts,
+                      splat_stream_t stream) {
+    if (int rc = validate(p)) return rc;
+    if (int rc = check_count(num_intersects)) return rc;
+    NEED(counts);
+    if (num_intersects > 0) {
+        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed); NEED(final_idx);
+        if (reinterpret_cast<uintptr_t>(packed) % 16)
+            return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
+    }
+    const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
+    return launch_count_pairs(*p, c, gaussian_ids_sorted, reinterpret_cast<const int2 *>(tile_bins),
+                              packed, final_idx, reinterpret_cast<unsigned long long *>(counts),
+                              (cudaStream_t)stream);
 }
 
 int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,

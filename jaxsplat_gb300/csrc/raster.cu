@@ -936,6 +936,99 @@ int launch_batch_raster_bwd(const splat_batch &b, Count count, const int32_t *id
     return check_launch("raster_bwd_batch_kernel");
 }
 
+// ---------------------------------------------------------------------------
+// Work counts for the compute roofline (diagnostic; not on the step path).
+// One block per tile, one thread per pixel (row-major), every list entry in
+// order, with the reference's per-pixel semantics and no culling:
+//   [0] pairs the forward evaluates: per pixel, entries up to and including
+//       the one that saturates it (forward.cu:380-455);
+//   [1] pairs the backward evaluates: entries up to the pixel's final_idx
+//       (backward.cu:240-262);
+//   [2] of those, the contributing ones (sigma >= 0 and alpha >= 1/255);
+//   [3] (tile, Gaussian) pairs with at least one contributing pixel (the
+//       granularity of the reference's gradient atomics, backward.cu:314-340).
+
+struct CountArgs {
+    unsigned tiles_x, width, height, bw;
+    int n;
+    Count count;
+    const int32_t *ids;
+    const int2 *bins;
+    const float4 *rec;
+    const int32_t *final_idx;
+    unsigned long long *counts;
+};
+
+__global__ void __launch_bounds__(kMaxTile) count_pairs_kernel(CountArgs a) {
+    __shared__ unsigned s_sum[3][kMaxWarps];
+    const int tile = (int)(blockIdx.y * a.tiles_x + blockIdx.x);
+    const int tr = threadIdx.x, lane = tr & 31, warp = tr >> 5;
+    const int bsize = (int)(a.bw * a.bw), nwarps = (bsize + 31) >> 5;
+    const unsigned i = blockIdx.y * a.bw + tr / a.bw, j = blockIdx.x * a.bw + tr % a.bw;
+    const bool inside = i < a.height && j < a.width;
+    const float px = (float)j + 0.5f, py = (float)i + 0.5f;
+    if (a.count.get() == 0) return;
+    const int2 range = a.bins[tile];
+    const int fidx = inside ? a.final_idx[(size_t)i * a.width + j] : -1;
+    bool done = !inside;
+    float T = 1.f;
+    unsigned e_fwd = 0, e_bwd = 0, e_valid = 0, e_tile = 0;
+    for (int e = range.x; e < range.y; ++e) {
+        const int g = a.ids[e];
+        bool valid = false;
+        if (g >= 0 && g < a.n && inside && (!done || e <= fidx)) {
+            const float4 r0 = a.rec[3 * (size_t)g], r1 = a.rec[3 * (size_t)g + 1];
+            const float sigma = falloff(r0.z, r0.w, r1.x, r0.x - px, r0.y - py);
+            const float vis = __expf(-sigma);
+            if (!done) {
+                ++e_fwd;
+                const float alpha = fminf(0.999f, r1.y * vis);
+                if (sigma >= 0.f && alpha >= 1.f / 255.f) {
+                    const float next_T = T * (1.f - alpha);
+                    if (next_T <= 1e-4f) done = true;
+                    else T = next_T;
+                }
+            }
+            if (e <= fidx) {
+                ++e_bwd;
+                const float alpha = fminf(0.99f, r1.y * vis);
+                valid = sigma >= 0.f && alpha >= 1.f / 255.f;
+                e_valid += valid;
+            }
+        }
+        if (__syncthreads_or(valid) && tr == 0) ++e_tile;
+    }
+    unsigned v[3] = {e_fwd, e_bwd, e_valid};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        unsigned x = v[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) s_sum[q][warp] = x;
+    }
+    __syncthreads();
+    if (tr < 3) {
+        unsigned long long t = 0;
+        for (int w = 0; w < nwarps; ++w) t += s_sum[tr][w];
+        atomicAdd(&a.counts[tr], t);
+    }
+    if (tr == 0) atomicAdd(&a.counts[3], (unsigned long long)e_tile);
+}
+
+int launch_count_pairs(const splat_params &p, Count count, const int32_t *ids, const int2 *bins,
+                       const float *rec, const int32_t *final_idx, unsigned long long *counts,
+                       cudaStream_t s) {
+    if (cudaMemsetAsync(counts, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess)
+        return check_launch("count_pairs memset");
+    if (count.cap == 0) return SPLAT_OK;
+    CountArgs a;
+    a.tiles_x = tiles_x(p); a.width = p.img_width; a.height = p.img_height; a.bw = p.block_width;
+    a.n = (int)p.num_points; a.count = count; a.ids = ids; a.bins = bins;
+    a.rec = reinterpret_cast<const float4 *>(rec); a.final_idx = final_idx; a.counts = counts;
+    dim3 grid(tiles_x(p), tiles_y(p));
+    count_pairs_kernel<<<grid, p.block_width * p.block_width, 0, s>>>(a);
+    return check_launch("count_pairs_kernel");
+}
+
 int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,
                       const int2 *bins, const float *rec, const float *background,
                       float *final_Ts, int32_t *final_idx, float *img, cudaStream_t s) {

@@ -206,6 +206,21 @@ class RenderSession:
             P(self.v_quat), P(self.v_cov2d), P(self.v_cov3d), s), "project_bwd")
         mark("end")
 
+    def count_pairs(self):
+        """Work counts of the last step (diagnostic, synchronises): pixel-Gaussian
+        pairs the reference's forward and backward evaluate, the contributing
+        ones, and (tile, Gaussian) pairs with a contributing pixel
+        (splat_count_pairs)."""
+        out = torch.zeros(4, dtype=torch.int64, device=self.dev)
+        P = self._p
+        self._check(self.lib.splat_count_pairs(
+            C.byref(self.params), self.capacity, P(self.total), P(self.ids_sorted),
+            P(self.tile_bins), P(self.packed), P(self.final_idx), P(out), self._stream()),
+            "count_pairs")
+        c = [int(x) for x in out.cpu().tolist()]
+        return {"fwd_evaluated": c[0], "bwd_evaluated": c[1], "bwd_contributing": c[2],
+                "tile_gaussian_contributing": c[3]}
+
     def _split(self, buf, first):
         """Offset in `buf` (a block) of the view named `first`."""
         return (getattr(self, first).data_ptr() - buf.data_ptr()) // 4
