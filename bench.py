@@ -121,7 +121,9 @@ class OursStep:
     """The render path through libsplat's C ABI, as one preallocated,
     sync-free step (jaxsplat_gb300.RenderSession) replayed as a CUDA graph."""
 
-    STAGES = ["project_fwd", "sort", "raster_fwd", "l2_loss", "raster_bwd", "project_bwd", "end"]
+    # the L2 loss runs inside the forward rasterizer; the packing pass runs on
+    # a second stream during the sort
+    STAGES = ["project_fwd", "sort", "raster_fwd", "raster_bwd", "project_bwd", "end"]
 
     def __init__(self, sc, dev, graph=True):
         import torch
@@ -155,8 +157,8 @@ class OursStep:
         tile_passes = (max(1, (tiles - 1).bit_length()) + 7) // 8
         # project, depth keys, 4-pass depth sort (+hist, offsets), emission
         # (offsets, expansion), tile sort (+hist, offsets), bins, pack, raster
-        # fwd, loss, raster bwd, project bwd
-        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 1 + 1 + 1 + 1
+        # fwd (+ loss), raster bwd, project bwd
+        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 1 + 1 + 1
         self.passes = tile_passes
 
     def launches_per_step(self):
@@ -167,14 +169,16 @@ class OursStep:
         intersection, 32 B per pixel and 9 fp32 atomics (36 B) per
         contributing (tile, Gaussian) pair I_c, counted by splat_count_pairs
         (`pairs`, when taken); raster forward: 40 B per intersection and 20 B
-        per pixel, plus the packing pass (36 B in + 48 B out per Gaussian)."""
+        per pixel, plus the fused L2 loss (target in, v_img out: 24 B per
+        pixel); the sort stage includes the packing pass that runs beside it
+        (36 B in + 48 B out per Gaussian)."""
         n, I = self.sc.spec.num_points, self.count
         h, w = self.sc.spec.img_shape
         P = h * w
         ic = (getattr(self, "pairs", None) or {}).get("tile_gaussian_contributing", 0)
-        return {"raster_bwd": 52 * I + 32 * P + 36 * ic, "raster_fwd": 40 * I + 20 * P + 84 * n,
-                "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes,
-                "project_fwd": 100 * n, "project_bwd": 140 * n, "l2_loss": 36 * P}
+        return {"raster_bwd": 52 * I + 32 * P + 36 * ic, "raster_fwd": 40 * I + 44 * P,
+                "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes + 84 * n,
+                "project_fwd": 100 * n, "project_bwd": 140 * n}
 
     def ncu_traffic(self, kernel):
         """Measured DRAM bytes of one launch (ncu), for the 1080p scene only."""
@@ -259,7 +263,7 @@ class BatchStep:
     views in one pass of each kernel (jaxsplat_gb300.BatchSession), one CUDA
     graph per step."""
 
-    STAGES = OursStep.STAGES
+    STAGES = ["project_fwd", "sort", "raster_fwd", "l2_loss", "raster_bwd", "project_bwd", "end"]
 
     def __init__(self, seed, dev, graph=True, autotune=False, log=None, points=None):
         import torch

@@ -100,6 +100,21 @@ SPLAT_API int splat_project_fwd(const splat_params *p, const float *means3d, con
                       int32_t *num_tiles_hit, int32_t *cum_tiles_hit, int64_t *total_out,
                       void *workspace, size_t workspace_bytes, splat_stream_t stream);
 
+/* splat_project_fwd that also writes the rasterizers' packed records
+ * (splat_pack_splats' output, bit-identical) from each Gaussian's projection
+ * and its colour and opacity, so that no separate packing pass runs.  No
+ * reference counterpart (the reference has no packing pass).  Same workspace.
+ *   colors (N,3) opacities (N,1) -> packed (N,12), 16-byte aligned */
+SPLAT_API int splat_project_fwd_packed(const splat_params *p, const float *means3d,
+                                       const float *scales, const float *quats,
+                                       const float *viewmat, const float *colors,
+                                       const float *opacities, float *cov3d, float *xys,
+                                       float *depths, int32_t *radii, float *conics,
+                                       float *compensation, int32_t *num_tiles_hit,
+                                       int32_t *cum_tiles_hit, int64_t *total_out,
+                                       float *packed, void *workspace, size_t workspace_bytes,
+                                       splat_stream_t stream);
+
 /* Blocking read of the intersection count and, when status_dev is not NULL,
  * of the device status word (which is then cleared).  Replaces the D2H read
  * in lib/ops.cu:424-432.  total_dev: the int64 written by splat_project_fwd;
@@ -158,6 +173,20 @@ SPLAT_API int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects,
                                   const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
                                   const float *packed, const float *background, float *final_Ts,
                                   int32_t *final_idx, float *out_img, splat_stream_t stream);
+
+/* splat_rasterize_fwd with the L2 loss of splat_l2_loss fused into its
+ * epilogue (each pixel's colour is still in registers): additionally
+ *   target (H,W,3) -> v_img (H,W,3) = 2 (img - target) / (3 H W), bit-identical
+ *   to splat_l2_loss's, and loss_out[0] = mean((img - target)^2) (overwritten;
+ *   summed per tile, so its last bits depend on the order of the tiles' adds,
+ *   as splat_l2_loss's do on its blocks'). */
+SPLAT_API int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersects,
+                                     const int64_t *count_dev,
+                                     const int32_t *gaussian_ids_sorted,
+                                     const int32_t *tile_bins, const float *packed,
+                                     const float *background, const float *target,
+                                     float *final_Ts, int32_t *final_idx, float *out_img,
+                                     float *v_img, float *loss_out, splat_stream_t stream);
 
 /* Rasterize backward over the same sorted list (no re-sort).  Replaces the
  * rasterize_bwd launch of ops::rasterize::bwd::xla (lib/ops.cu:203-225,

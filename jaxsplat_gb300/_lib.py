@@ -78,12 +78,14 @@ _SIGS = [
     ("splat_version", C.c_int, []),
     ("splat_project_fwd_workspace_size", C.c_size_t, [_P]),
     ("splat_project_fwd", C.c_int, [_P] + [_v] * 13 + [_v, C.c_size_t, _v]),
+    ("splat_project_fwd_packed", C.c_int, [_P] + [_v] * 16 + [_v, C.c_size_t, _v]),
     ("splat_read_counts", C.c_int, [_P, _v, _v, _v, C.POINTER(C.c_int64),
                                     C.POINTER(C.c_uint32), _v]),
     ("splat_sort_workspace_size", C.c_size_t, [_P, C.c_int64]),
     ("splat_sort_and_bin", C.c_int, [_P, C.c_int64] + [_v] * 10 + [_v, C.c_size_t, _v]),
     ("splat_pack_splats", C.c_int, [_P] + [_v] * 5 + [_v]),
     ("splat_rasterize_fwd", C.c_int, [_P, C.c_int64] + [_v] * 8 + [_v]),
+    ("splat_rasterize_fwd_l2", C.c_int, [_P, C.c_int64] + [_v] * 11 + [_v]),
     ("splat_rasterize_bwd", C.c_int, [_P, C.c_int64] + [_v] * 14 + [_v]),
     ("splat_project_bwd", C.c_int, [_P] + [_v] * 17 + [_v]),
     ("splat_l2_loss", C.c_int, [_v, _v, C.c_int64, _v, _v, _v]),

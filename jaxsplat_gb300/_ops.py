@@ -63,9 +63,10 @@ def _workspace(nbytes: int, device) -> torch.Tensor:
 # project
 
 def project_fwd(means3d, scales, quats, viewmat, *, img_shape, f, c, glob_scale, clip_thresh,
-                block_width):
+                block_width, colors=None, opacities=None):
     """lib/ops.cu:12-61 -> dict(cov3d, xys, depths, radii, conics, compensation,
-    num_tiles_hit, cum_tiles_hit, total)."""
+    num_tiles_hit, cum_tiles_hit, total); with colors and opacities also the
+    packed rasterizer records ("packed", splat_project_fwd_packed)."""
     lib = _lib.load()
     n = means3d.shape[0]
     dev = means3d.device
@@ -83,12 +84,25 @@ def project_fwd(means3d, scales, quats, viewmat, *, img_shape, f, c, glob_scale,
                num_tiles_hit=torch.empty(n, 1, **i32), cum_tiles_hit=torch.empty(n, 1, **i32),
                total=torch.empty(1, dtype=torch.int64, device=dev))
     ws = _workspace(lib.splat_project_fwd_workspace_size(C.byref(p)), dev)
-    rc = lib.splat_project_fwd(
-        C.byref(p), _ptr(means3d), _ptr(scales), _ptr(quats), _ptr(viewmat), _ptr(out["cov3d"]),
-        _ptr(out["xys"]), _ptr(out["depths"]), _ptr(out["radii"]), _ptr(out["conics"]),
-        _ptr(out["compensation"]), _ptr(out["num_tiles_hit"]), _ptr(out["cum_tiles_hit"]),
-        _ptr(out["total"]), _ptr(ws), ws.numel(), _stream())
-    _lib.check(rc, "project_fwd")
+    if colors is None:
+        rc = lib.splat_project_fwd(
+            C.byref(p), _ptr(means3d), _ptr(scales), _ptr(quats), _ptr(viewmat),
+            _ptr(out["cov3d"]), _ptr(out["xys"]), _ptr(out["depths"]), _ptr(out["radii"]),
+            _ptr(out["conics"]), _ptr(out["compensation"]), _ptr(out["num_tiles_hit"]),
+            _ptr(out["cum_tiles_hit"]), _ptr(out["total"]), _ptr(ws), ws.numel(), _stream())
+        _lib.check(rc, "project_fwd")
+        return out
+    _check_type(colors, (n, 3), torch.float32, "colors")
+    _check_type(opacities, (n, 1), torch.float32, "opacities")
+    colors, opacities = _contig(colors), _contig(opacities)
+    out["packed"] = torch.empty(n, 12, **f32)
+    rc = lib.splat_project_fwd_packed(
+        C.byref(p), _ptr(means3d), _ptr(scales), _ptr(quats), _ptr(viewmat), _ptr(colors),
+        _ptr(opacities), _ptr(out["cov3d"]), _ptr(out["xys"]), _ptr(out["depths"]),
+        _ptr(out["radii"]), _ptr(out["conics"]), _ptr(out["compensation"]),
+        _ptr(out["num_tiles_hit"]), _ptr(out["cum_tiles_hit"]), _ptr(out["total"]),
+        _ptr(out["packed"]), _ptr(ws), ws.numel(), _stream())
+    _lib.check(rc, "project_fwd_packed")
     return out
 
 
@@ -188,6 +202,30 @@ def rasterize_fwd(num_intersects, ids_sorted, tile_bins, packed, background, *, 
                                  _ptr(out["final_Ts"]), _ptr(out["final_idx"]), _ptr(out["img"]),
                                  _stream())
     _lib.check(rc, "rasterize_fwd")
+    return out
+
+
+def rasterize_fwd_l2(num_intersects, ids_sorted, tile_bins, packed, background, target, *,
+                     img_shape, block_width, count_dev=None):
+    """rasterize_fwd with the L2 loss against `target` fused in (include/splat.h
+    splat_rasterize_fwd_l2) -> dict(final_Ts, final_idx, img, v_img, loss)."""
+    lib = _lib.load()
+    n = packed.shape[0]
+    dev = packed.device
+    p = _params(n, img_shape, block_width=block_width, device=dev)
+    h, w = img_shape
+    f32 = dict(dtype=torch.float32, device=dev)
+    out = dict(final_Ts=torch.empty(h, w, 1, **f32),
+               final_idx=torch.empty(h, w, 1, dtype=torch.int32, device=dev),
+               img=torch.empty(h, w, 3, **f32), v_img=torch.empty(h, w, 3, **f32),
+               loss=torch.empty(1, **f32))
+    _check_type(target, (h, w, 3), torch.float32, "target")
+    args = [_contig(t) for t in (ids_sorted, tile_bins, packed, background, target)]
+    rc = lib.splat_rasterize_fwd_l2(C.byref(p), num_intersects, _ptr(count_dev),
+                                    *[_ptr(t) for t in args], _ptr(out["final_Ts"]),
+                                    _ptr(out["final_idx"]), _ptr(out["img"]), _ptr(out["v_img"]),
+                                    _ptr(out["loss"]), _stream())
+    _lib.check(rc, "rasterize_fwd_l2")
     return out
 
 

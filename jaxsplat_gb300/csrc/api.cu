@@ -11,7 +11,8 @@ namespace splat {
 // kernels implemented in project.cu / sort.cu / raster.cu
 int launch_project_fwd(const splat_params &, const float *, const float *, const float *,
                        const float *, float *, float *, float *, int32_t *, float *, float *,
-                       int32_t *, int32_t *, int64_t *, unsigned long long *, cudaStream_t);
+                       int32_t *, int32_t *, int64_t *, unsigned long long *, const float *, const float *, float *,
+                       cudaStream_t);
 int launch_project_bwd(const splat_params &, const float *, const float *, const float *,
                        const float *, const float *, const int32_t *, const float *,
                        const float *, const float *, const float *, const float *,
@@ -23,7 +24,8 @@ int launch_sort_and_bin(const splat_params &, Count, const float *, const float 
 int launch_pack(const splat_params &, const float *, const float *, const float *, const float *,
                 float *, cudaStream_t);
 int launch_raster_fwd(const splat_params &, Count, const int32_t *, const int2 *,
-                      const float *, const float *, float *, int32_t *, float *, cudaStream_t);
+                      const float *, const float *, float *, int32_t *, float *, const float *,
+                      float *, float *, cudaStream_t);
 int launch_raster_bwd(const splat_params &, Count, const int32_t *, const int2 *,
                       const float *, const float *, const float *, const int32_t *,
                       const float *, const float *, float *, float *, float *, float *, float *,
@@ -209,11 +211,16 @@ size_t splat_project_fwd_workspace_size(const splat_params *p) {
     return p ? project_ws_bytes(*p) : 0;
 }
 
-int splat_project_fwd(const splat_params *p, const float *means3d, const float *scales,
-                      const float *quats, const float *viewmat, float *cov3d, float *xys,
-                      float *depths, int32_t *radii, float *conics, float *compensation,
-                      int32_t *num_tiles_hit, int32_t *cum_tiles_hit, int64_t *total_out,
-                      void *workspace, size_t workspace_bytes, splat_stream_t stream) {
+}  // extern "C"
+
+// splat_project_fwd, and with colors / opacities / packed non-null also the
+// packed records (splat_project_fwd_packed).
+static int project_fwd_entry(const splat_params *p, const float *means3d, const float *scales,
+                             const float *quats, const float *viewmat, float *cov3d, float *xys,
+                             float *depths, int32_t *radii, float *conics, float *compensation,
+                             int32_t *num_tiles_hit, int32_t *cum_tiles_hit, int64_t *total_out,
+                             void *workspace, size_t workspace_bytes, const float *colors,
+                             const float *opacities, float *packed, splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (p->num_points == 0) {
@@ -233,7 +240,37 @@ int splat_project_fwd(const splat_params *p, const float *means3d, const float *
     unsigned long long *words = ar.take<unsigned long long>(parts + 1);
     return launch_project_fwd(*p, means3d, scales, quats, viewmat, cov3d, xys, depths, radii,
                               conics, compensation, num_tiles_hit, cum_tiles_hit,
-                              total_out ? total_out : total_slot, words, s);
+                              total_out ? total_out : total_slot, words, colors, opacities,
+                              packed, s);
+}
+
+extern "C" {
+
+int splat_project_fwd(const splat_params *p, const float *means3d, const float *scales,
+                      const float *quats, const float *viewmat, float *cov3d, float *xys,
+                      float *depths, int32_t *radii, float *conics, float *compensation,
+                      int32_t *num_tiles_hit, int32_t *cum_tiles_hit, int64_t *total_out,
+                      void *workspace, size_t workspace_bytes, splat_stream_t stream) {
+    return project_fwd_entry(p, means3d, scales, quats, viewmat, cov3d, xys, depths, radii,
+                             conics, compensation, num_tiles_hit, cum_tiles_hit, total_out,
+                             workspace, workspace_bytes, nullptr, nullptr, nullptr, stream);
+}
+
+int splat_project_fwd_packed(const splat_params *p, const float *means3d, const float *scales,
+                             const float *quats, const float *viewmat, const float *colors,
+                             const float *opacities, float *cov3d, float *xys, float *depths,
+                             int32_t *radii, float *conics, float *compensation,
+                             int32_t *num_tiles_hit, int32_t *cum_tiles_hit, int64_t *total_out,
+                             float *packed, void *workspace, size_t workspace_bytes,
+                             splat_stream_t stream) {
+    if (p && p->num_points > 0) {
+        NEED(colors); NEED(opacities); NEED(packed);
+        if (reinterpret_cast<uintptr_t>(packed) % 16)
+            return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
+    }
+    return project_fwd_entry(p, means3d, scales, quats, viewmat, cov3d, xys, depths, radii,
+                             conics, compensation, num_tiles_hit, cum_tiles_hit, total_out,
+                             workspace, workspace_bytes, colors, opacities, packed, stream);
 }
 
 int splat_read_counts(const splat_params *p, const int32_t *cum_tiles_hit,
@@ -319,7 +356,29 @@ int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int
     const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
     return launch_raster_fwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
-                             final_Ts, final_idx, out_img, (cudaStream_t)stream);
+                             final_Ts, final_idx, out_img, nullptr, nullptr, nullptr,
+                             (cudaStream_t)stream);
+}
+
+int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
+                           const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                           const float *packed, const float *background, const float *target,
+                           float *final_Ts, int32_t *final_idx, float *out_img, float *v_img,
+                           float *loss_out, splat_stream_t stream) {
+    if (int rc = validate(p)) return rc;
+    if (int rc = check_count(num_intersects)) return rc;
+    NEED(background); NEED(target); NEED(final_Ts); NEED(final_idx); NEED(out_img);
+    NEED(v_img); NEED(loss_out);
+    if (num_intersects > 0) {
+        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed);
+        if (reinterpret_cast<uintptr_t>(packed) % 16)
+            return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
+    }
+    const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
+    return launch_raster_fwd(*p, c, gaussian_ids_sorted,
+                             reinterpret_cast<const int2 *>(tile_bins), packed, background,
+                             final_Ts, final_idx, out_img, target, v_img, loss_out,
+                             (cudaStream_t)stream);
 }
 
 int splat_count_pairs(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,

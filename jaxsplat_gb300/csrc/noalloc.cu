@@ -25,7 +25,8 @@ namespace splat {
 
 int launch_project_fwd(const splat_params &, const float *, const float *, const float *,
                        const float *, float *, float *, float *, int32_t *, float *, float *,
-                       int32_t *, int32_t *, int64_t *, unsigned long long *, cudaStream_t);
+                       int32_t *, int32_t *, int64_t *, unsigned long long *, const float *, const float *, float *,
+                       cudaStream_t);
 int check_params(const splat_params *p);
 
 constexpr uint32_t kNoAllocMaxPoints = 1u << 24;
@@ -100,5 +101,5 @@ extern "C" int splat_project_fwd_noalloc(const splat_params *p, const float *mea
     // before the kernel reads them.
     return launch_project_fwd(*p, means3d, scales, quats, viewmat, cov3d, xys, depths, radii,
                               conics, compensation, num_tiles_hit, cum_tiles_hit, total, scratch,
-                              s);
+                              nullptr, nullptr, nullptr, s);
 }

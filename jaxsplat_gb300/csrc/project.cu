@@ -36,6 +36,11 @@ struct ProjFwdArgs {
     uint32_t *status;
     uint32_t spin_limit;
     int rounds;  // rounds of kProjThreads Gaussians per partition, 1..kProjRounds
+    // optional (rec non-null): the rasterizers' record of each Gaussian
+    // (write_record) from its projection and its colour and opacity, which
+    // makes the separate packing pass unnecessary
+    const float *colors, *opac;
+    float4 *rec;
 };
 
 // Inclusive scan over the block of one value per thread; returns the
@@ -102,6 +107,11 @@ __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a
             a.conics[3 * (size_t)i + 2] = o.conic.z;
             a.comp[i] = o.comp;
             a.ntiles[i] = (int32_t)hits;
+            if (a.rec)
+                write_record(a.rec + 3 * (size_t)i, o.center, o.conic, a.opac[i],
+                             make_float3(a.colors[3 * (size_t)i], a.colors[3 * (size_t)i + 1],
+                                         a.colors[3 * (size_t)i + 2]),
+                             0.f);
         }
         unsigned long long round_total;
         incl[r] = run + block_scan(hits, s_warp, &round_total);
@@ -180,11 +190,13 @@ __global__ void __launch_bounds__(256) project_bwd_kernel(ProjBwdArgs a) {
 // ---------------------------------------------------------------------------
 // Host launchers.
 
+// colors / opac / rec non-null: the packed records are written too.
 int launch_project_fwd(const splat_params &p, const float *means3d, const float *scales,
                        const float *quats, const float *viewmat, float *cov3d, float *xys,
                        float *depths, int32_t *radii, float *conics, float *comp,
                        int32_t *ntiles, int32_t *cum, int64_t *total,
-                       unsigned long long *words, cudaStream_t s) {
+                       unsigned long long *words, const float *colors, const float *opac,
+                       float *rec, cudaStream_t s) {
     const int n = (int)p.num_points;
     // rounds per partition: as few as keep the partitions within one wave of
     // two blocks per SM, at most 8
@@ -209,6 +221,7 @@ int launch_project_fwd(const splat_params &p, const float *means3d, const float 
     a.status = p.device_status;
     a.spin_limit = spin_limit(p);
     a.rounds = rounds;
+    a.colors = colors; a.opac = opac; a.rec = reinterpret_cast<float4 *>(rec);
     project_fwd_kernel<<<nparts, kProjThreads, 0, s>>>(a);
     return check_launch("project_fwd_kernel");
 }

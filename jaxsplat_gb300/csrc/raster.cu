@@ -37,34 +37,8 @@ constexpr int kMaxTile = 256;  // bw * bw <= 256
 constexpr int kMaxWarps = kMaxTile / 32;
 
 // ---------------------------------------------------------------------------
-// Packing.
-//
-// Record (3 x float4):  r0 = (x, y, conic a, conic b)
-//                       r1 = (conic c, opacity, red, green)
-//                       r2 = (blue, hx, hy, tag)
-// (tag: 0 for a single view; for batched views the scene Gaussian's index,
-// as int bits, that receives the colour and opacity gradients.)
-// Outside the box |px - x| <= hx, |py - y| <= hy no pixel centre passes the
-// test alpha >= 1/255 in the rasterizers' fp32 arithmetic.  hx = +inf means
-// "no bound proven" (never culled); hx = -inf means "no pixel anywhere".
-//
-// Why the box is safe: for a positive-definite conic A the exact exponent is
-// sigma = d^T A d / 2, and alpha >= 1/255 needs sigma <= thr = ln(255 o).
-// The ellipse d^T A d <= q has half-extents sqrt(q (A^-1)_xx), sqrt(q (A^-1)_yy)
-// with (A^-1)_xx = c / det, (A^-1)_yy = a / det.  The fp32 exponent differs
-// from the exact one by at most 12 kappa 2^-24 of it, kappa = the condition
-// number <= tr^2 / det; boxes are only built when tr^2 / det <= 1e4, so that
-// is below 1% and q = 2 (thr + 0.01) / 0.98 covers it, the 0.01 absorbing the
-// error of __expf and of the product o * exp.  det is formed with Kahan's
-// error-free 2x2 determinant (within 2 ulp however much a c and b^2 cancel);
-// logf and sqrtf are within 1 ulp; the half-extents get a further 0.1% and
-// 0.01 px, and Gaussians centred more than 1e5 px away are never culled, so
-// fp32 rounding of x +- hx cannot shrink the box.
-
-constexpr float kCullMargin = 0.01f;
-constexpr float kCullSigmaFactor = 0.98f;
-constexpr float kCullMaxCond = 1e4f;
-constexpr float kCullFarPx = 1e5f;
+// Packing: one 48-byte record per Gaussian (write_record in splat_math.cuh,
+// with the record layout and the proof of its culling box).
 
 struct PackArgs {
     int n;
@@ -76,35 +50,9 @@ struct PackArgs {
 // last word carries gc (as int bits) for the batched backward.
 __device__ __forceinline__ void pack_record(const PackArgs &a, size_t i, size_t gc, float tag) {
     const float2 xy = *reinterpret_cast<const float2 *>(a.xys + 2 * i);
-    const float ca = a.conics[3 * i], cb = a.conics[3 * i + 1], cc = a.conics[3 * i + 2];
-    const float o = a.opac[gc];
-    const float cr = a.colors[3 * gc], cg = a.colors[3 * gc + 1], cbl = a.colors[3 * gc + 2];
-    float hx = CUDART_INF_F, hy = CUDART_INF_F;
-    // det = a c - b^2 (Kahan): w = b*b rounded, e = its rounding error
-    const float w = cb * cb;
-    const float e = fmaf(cb, cb, -w);
-    const float det = fmaf(ca, cc, -w) - e;
-    const float trc = ca + cc;
-    const bool finite = isfinite(xy.x) && isfinite(xy.y) && fabsf(xy.x) < kCullFarPx &&
-                        fabsf(xy.y) < kCullFarPx && isfinite(o) && isfinite(ca) &&
-                        isfinite(cb) && isfinite(cc) && isfinite(det);
-    if (finite && ca > 0.f && cc > 0.f && det > 0.f && trc * trc <= kCullMaxCond * det && o > 0.f) {
-        const float q = 2.f * (logf(255.f * o) + kCullMargin) / kCullSigmaFactor;
-        if (q <= 0.f) {
-            hx = hy = -CUDART_INF_F;
-        } else {
-            const float ex = sqrtf(q * cc / det) * 1.001f + 0.01f;
-            const float ey = sqrtf(q * ca / det) * 1.001f + 0.01f;
-            if (ex < kCullFarPx && ey < kCullFarPx) {
-                hx = ex;
-                hy = ey;
-            }
-        }
-    }
-    float4 *r = a.rec + 3 * i;
-    r[0] = make_float4(xy.x, xy.y, ca, cb);
-    r[1] = make_float4(cc, o, cr, cg);
-    r[2] = make_float4(cbl, hx, hy, tag);
+    const float3 conic = make_float3(a.conics[3 * i], a.conics[3 * i + 1], a.conics[3 * i + 2]);
+    const float3 rgb = make_float3(a.colors[3 * gc], a.colors[3 * gc + 1], a.colors[3 * gc + 2]);
+    write_record(a.rec + 3 * i, xy, conic, a.opac[gc], rgb, tag);
 }
 
 __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
@@ -252,9 +200,51 @@ struct RasterFwdArgs {
     float *final_Ts;
     int32_t *final_idx;
     float *img;
+    // kLoss: the L2 loss against `target` (same layout as img), as
+    // splat_l2_loss computes it: v_img = 2 (img - target) / count, and the
+    // tile's share of mean((img - target)^2) added to *loss
+    const float *target;
+    float *v_img, *loss;
+    float inv_count;
 };
 
-template <bool k8x4>
+// The L2 loss terms of one pixel (inside the image); returns its squared error.
+__device__ __forceinline__ float pixel_l2(const RasterFwdArgs &a, size_t pix, float r, float g,
+                                          float b) {
+    const float v[3] = {r, g, b};
+    float sq = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float d = v[k] - a.target[3 * pix + k];
+        a.v_img[3 * pix + k] = 2.f * d * a.inv_count;
+        sq += d * d;
+    }
+    return sq;
+}
+
+// Block sum of the squared errors, one atomic per tile.  Warp 0 sums the
+// staged values (a block of fewer than 32 threads: thread 0 alone).
+__device__ __forceinline__ void tile_l2_sum(const RasterFwdArgs &a, float sq, int bsize) {
+    __shared__ float s_sq[kMaxTile];
+    const int tr = threadIdx.x;
+    s_sq[tr] = sq;
+    __syncthreads();
+    if (bsize >= 32) {
+        if (tr < 32) {
+            float t = 0.f;
+            for (int k = tr; k < bsize; k += 32) t += s_sq[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (tr == 0) atomicAdd(a.loss, t * a.inv_count);
+        }
+    } else if (tr == 0) {
+        float t = 0.f;
+        for (int k = 0; k < bsize; ++k) t += s_sq[k];
+        atomicAdd(a.loss, t * a.inv_count);
+    }
+}
+
+template <bool k8x4, bool kLoss = false>
 __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &c) {
     __shared__ float4 s_r0[kMaxTile];
     __shared__ float4 s_r1[kMaxTile];
@@ -279,13 +269,16 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
     const float3 bg = c.bg;
 
     if (a.count.get() == 0) {  // lib/ops.cu:119-127: background image, zero T and index
+        float sq = 0.f;
         if (inside) {
             a.final_Ts[pix] = 0.f;
             a.final_idx[pix] = 0;
             a.img[3 * pix] = bg.x;
             a.img[3 * pix + 1] = bg.y;
             a.img[3 * pix + 2] = bg.z;
+            if (kLoss) sq = pixel_l2(a, pix, bg.x, bg.y, bg.z);
         }
+        if (kLoss) tile_l2_sum(a, sq, bsize);
         return;
     }
     if (tr < nwarps) s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
@@ -336,18 +329,22 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
             cur_idx = start + t;
         }
     }
+    float sq = 0.f;
     if (inside) {
         a.final_Ts[pix] = T;
         a.final_idx[pix] = cur_idx;
-        a.img[3 * pix] = blend(acc.x, T, bg.x);
-        a.img[3 * pix + 1] = blend(acc.y, T, bg.y);
-        a.img[3 * pix + 2] = blend(acc.z, T, bg.z);
+        const float r = blend(acc.x, T, bg.x), g = blend(acc.y, T, bg.y), b = blend(acc.z, T, bg.z);
+        a.img[3 * pix] = r;
+        a.img[3 * pix + 1] = g;
+        a.img[3 * pix + 2] = b;
+        if (kLoss) sq = pixel_l2(a, pix, r, g, b);
     }
+    if (kLoss) tile_l2_sum(a, sq, bsize);
 }
 
-template <bool k8x4>
+template <bool k8x4, bool kLoss>
 __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
-    fwd_tile<k8x4>(a, grid_tile(a.tiles_x, a.bw, a.width, a.height, a.background));
+    fwd_tile<k8x4, kLoss>(a, grid_tile(a.tiles_x, a.bw, a.width, a.height, a.background));
 }
 
 // ---------------------------------------------------------------------------
@@ -889,6 +886,7 @@ int launch_batch_raster_fwd(const splat_batch &b, Count count, const int32_t *id
     a.count = count; a.ids = ids; a.bins = bins;
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = nullptr;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
+    a.target = nullptr; a.v_img = nullptr; a.loss = nullptr; a.inv_count = 0.f;
     const BatchTiles t = batch_tiles(b, order, chunk, next);
     const int threads = (int)(b.block_width * b.block_width);
     int grid = 0;
@@ -1029,21 +1027,32 @@ int launch_count_pairs(const splat_params &p, Count count, const int32_t *ids, c
     return check_launch("count_pairs_kernel");
 }
 
+// target / v_img / loss non-null: the L2 loss is fused into the epilogue.
 int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,
                       const int2 *bins, const float *rec, const float *background,
-                      float *final_Ts, int32_t *final_idx, float *img, cudaStream_t s) {
+                      float *final_Ts, int32_t *final_idx, float *img, const float *target,
+                      float *v_img, float *loss, cudaStream_t s) {
     RasterFwdArgs a;
     a.tiles_x = tiles_x(p); a.width = p.img_width; a.height = p.img_height; a.bw = p.block_width;
     a.n = (int)p.num_points; a.status = p.device_status;
     a.count = count; a.ids = ids; a.bins = bins;
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = background;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
+    a.target = target; a.v_img = v_img; a.loss = loss;
+    const long long npix3 = 3ll * p.img_width * p.img_height;
+    a.inv_count = npix3 > 0 ? 1.f / (float)npix3 : 0.f;
+    const bool fused = target != nullptr;
+    if (fused && cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess)
+        return check_launch("loss memset");
     dim3 grid(tiles_x(p), tiles_y(p));
     const unsigned threads = p.block_width * p.block_width;
-    if (p.block_width == 16)
-        raster_fwd_kernel<true><<<grid, threads, 0, s>>>(a);
-    else
-        raster_fwd_kernel<false><<<grid, threads, 0, s>>>(a);
+    if (p.block_width == 16) {
+        if (fused) raster_fwd_kernel<true, true><<<grid, threads, 0, s>>>(a);
+        else raster_fwd_kernel<true, false><<<grid, threads, 0, s>>>(a);
+    } else {
+        if (fused) raster_fwd_kernel<false, true><<<grid, threads, 0, s>>>(a);
+        else raster_fwd_kernel<false, false><<<grid, threads, 0, s>>>(a);
+    }
     return check_launch("raster_fwd_kernel");
 }
 

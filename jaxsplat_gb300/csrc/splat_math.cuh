@@ -11,6 +11,8 @@
 // structs, no cooperative-groups dependency.
 #pragma once
 
+#include <math_constants.h>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -207,5 +209,67 @@ __device__ __forceinline__ float falloff(float a, float b, float c, float dx, fl
 // pix_out + c * vis and acc + T * bg of forward.cu:443-459 (one fused
 // multiply-add each).
 __device__ __forceinline__ float blend(float acc, float c, float w) { return __fmaf_rn(c, w, acc); }
+
+// ---------------------------------------------------------------------------
+// Per-Gaussian rasterizer records.
+//
+//
+// Record (3 x float4):  r0 = (x, y, conic a, conic b)
+//                       r1 = (conic c, opacity, red, green)
+//                       r2 = (blue, hx, hy, tag)
+// (tag: 0 for a single view; for batched views the scene Gaussian's index,
+// as int bits, that receives the colour and opacity gradients.)
+// Outside the box |px - x| <= hx, |py - y| <= hy no pixel centre passes the
+// test alpha >= 1/255 in the rasterizers' fp32 arithmetic.  hx = +inf means
+// "no bound proven" (never culled); hx = -inf means "no pixel anywhere".
+//
+// Why the box is safe: for a positive-definite conic A the exact exponent is
+// sigma = d^T A d / 2, and alpha >= 1/255 needs sigma <= thr = ln(255 o).
+// The ellipse d^T A d <= q has half-extents sqrt(q (A^-1)_xx), sqrt(q (A^-1)_yy)
+// with (A^-1)_xx = c / det, (A^-1)_yy = a / det.  The fp32 exponent differs
+// from the exact one by at most 12 kappa 2^-24 of it, kappa = the condition
+// number <= tr^2 / det; boxes are only built when tr^2 / det <= 1e4, so that
+// is below 1% and q = 2 (thr + 0.01) / 0.98 covers it, the 0.01 absorbing the
+// error of __expf and of the product o * exp.  det is formed with Kahan's
+// error-free 2x2 determinant (within 2 ulp however much a c and b^2 cancel);
+// logf and sqrtf are within 1 ulp; the half-extents get a further 0.1% and
+// 0.01 px, and Gaussians centred more than 1e5 px away are never culled, so
+// fp32 rounding of x +- hx cannot shrink the box.
+
+constexpr float kCullMargin = 0.01f;
+constexpr float kCullSigmaFactor = 0.98f;
+constexpr float kCullMaxCond = 1e4f;
+constexpr float kCullFarPx = 1e5f;
+
+// The record of one Gaussian (xy, conic, opacity, colour; tag as above).
+__device__ __forceinline__ void write_record(float4 *r, float2 xy, float3 conic, float o,
+                                             float3 rgb, float tag) {
+    const float ca = conic.x, cb = conic.y, cc = conic.z;
+    float hx = CUDART_INF_F, hy = CUDART_INF_F;
+    // det = a c - b^2 (Kahan): w = b*b rounded, e = its rounding error
+    const float w = cb * cb;
+    const float e = fmaf(cb, cb, -w);
+    const float det = fmaf(ca, cc, -w) - e;
+    const float trc = ca + cc;
+    const bool finite = isfinite(xy.x) && isfinite(xy.y) && fabsf(xy.x) < kCullFarPx &&
+                        fabsf(xy.y) < kCullFarPx && isfinite(o) && isfinite(ca) &&
+                        isfinite(cb) && isfinite(cc) && isfinite(det);
+    if (finite && ca > 0.f && cc > 0.f && det > 0.f && trc * trc <= kCullMaxCond * det && o > 0.f) {
+        const float q = 2.f * (logf(255.f * o) + kCullMargin) / kCullSigmaFactor;
+        if (q <= 0.f) {
+            hx = hy = -CUDART_INF_F;
+        } else {
+            const float ex = sqrtf(q * cc / det) * 1.001f + 0.01f;
+            const float ey = sqrtf(q * ca / det) * 1.001f + 0.01f;
+            if (ex < kCullFarPx && ey < kCullFarPx) {
+                hx = ex;
+                hy = ey;
+            }
+        }
+    }
+    r[0] = make_float4(xy.x, xy.y, ca, cb);
+    r[1] = make_float4(cc, o, rgb.x, rgb.y);
+    r[2] = make_float4(rgb.z, hx, hy, tag);
+}
 
 }  // namespace splat

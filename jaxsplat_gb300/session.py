@@ -166,32 +166,42 @@ class RenderSession:
             P(self.ntiles), P(self.cum), P(self.total), P(self.proj_ws), self.proj_ws.numel(),
             self._stream()), "project_fwd")
 
-    def step(self, mark=None):
+    def step(self, mark=None, side=None):
         """Enqueue one forward+backward on the current stream (no host sync).
         ``mark(stage)`` is called before each stage and with "end" after the
-        last (e.g. to record CUDA events)."""
+        last (e.g. to record CUDA events).  The packing pass runs on a second
+        stream (``side``, or the session's own) while the sort runs; the
+        forward rasterizer computes the L2 loss in its epilogue."""
         if self.capacity is None:
             self.measure_capacity()
-        P, pr, s, cap = self._p, C.byref(self.params), self._stream(), self.capacity
+        P, pr, cap = self._p, C.byref(self.params), self.capacity
         lib = self.lib
+        cur = torch.cuda.current_stream(self.dev)
+        s = C.c_void_p(cur.cuda_stream)
+        if side is None:
+            side = self._pack_stream = (getattr(self, "_pack_stream", None)
+                                        or torch.cuda.Stream(self.dev))
         mark = mark or (lambda name: None)
         mark("project_fwd")
         self._project()
+        projected = torch.cuda.Event()
+        projected.record(cur)
+        side.wait_event(projected)
+        with torch.cuda.stream(side):
+            self._check(lib.splat_pack_splats(
+                pr, P(self.xys), P(self.conics), P(self.colors), P(self.opacities),
+                P(self.packed), C.c_void_p(side.cuda_stream)), "pack_splats")
         mark("sort")
         self._check(lib.splat_sort_and_bin(
             pr, cap, P(self.total), P(self.xys), P(self.depths), P(self.radii), P(self.cum),
             P(self.ids_sorted), P(self.tile_bins), None, None, None, P(self.sort_ws),
             self.sort_ws.numel(), s), "sort_and_bin")
+        cur.wait_stream(side)
         mark("raster_fwd")
-        self._check(lib.splat_pack_splats(pr, P(self.xys), P(self.conics), P(self.colors),
-                                          P(self.opacities), P(self.packed), s), "pack_splats")
-        self._check(lib.splat_rasterize_fwd(
+        self._check(lib.splat_rasterize_fwd_l2(
             pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),
-            P(self.background), P(self.final_Ts), P(self.final_idx), P(self.img), s),
-            "rasterize_fwd")
-        mark("l2_loss")
-        self._check(lib.splat_l2_loss(P(self.img), P(self.target), self.img.numel(),
-                                      P(self.loss), P(self.v_img), s), "l2_loss")
+            P(self.background), P(self.target), P(self.final_Ts), P(self.final_idx),
+            P(self.img), P(self.v_img), P(self.loss), s), "rasterize_fwd_l2")
         mark("raster_bwd")
         self._check(lib.splat_rasterize_bwd(
             pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),
@@ -241,19 +251,19 @@ class RenderSession:
         self.inputs[:a_in].copy_(host_in[:a_in], non_blocking=True)
         # the second half follows the first (copies in parallel would share the
         # link and delay the projection) but overlaps the projection and sort;
-        # waiting on `cur` also orders it after the previous step's readers
+        # waiting on `cur` also orders it after the previous step's readers.
+        # The packing pass follows it on the same stream, and the rasterizer
+        # waits for both.
         side.wait_stream(cur)
         with torch.cuda.stream(side):
             self.inputs[a_in:].copy_(host_in[a_in:], non_blocking=True)
         def mark(name):
-            if name == "raster_fwd":  # the rasterizer needs the second half
-                cur.wait_stream(side)
-            elif name == "project_bwd":  # colour/opacity gradients are final
+            if name == "project_bwd":  # colour/opacity gradients are final
                 side.wait_stream(cur)
                 with torch.cuda.stream(side):
                     host_out[:a_out].copy_(self.outputs[:a_out], non_blocking=True)
 
-        self.step(mark=mark)
+        self.step(mark=mark, side=side)
         host_out[a_out:].copy_(self.outputs[a_out:], non_blocking=True)
         cur.wait_stream(side)
 

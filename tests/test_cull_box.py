@@ -1,7 +1,7 @@
 """The rasterizers' per-Gaussian culling box must be conservative: no pixel
 centre outside it may pass the reference's test alpha >= 1/255 (evaluated
 in fp32 the way the kernels evaluate it).  This restates the box of
-pack_kernel (jaxsplat_gb300/csrc/raster.cu) in numpy and checks it by brute
+write_record (jaxsplat_gb300/csrc/splat_math.cuh) in numpy and checks it by brute
 force around random Gaussians, anisotropic and nearly degenerate ones
 included (CPU only)."""
 
