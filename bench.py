@@ -155,10 +155,10 @@ class OursStep:
         bw = sc.spec.block_width
         tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
         tile_passes = (max(1, (tiles - 1).bit_length()) + 7) // 8
-        # project, depth keys, 4-pass depth sort (+hist, offsets), emission
-        # (offsets, expansion), tile sort (+hist, offsets), bins, pack, raster
-        # fwd (+ loss), raster bwd, project bwd
-        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 1 + 1 + 1
+        # project (+ packing), depth keys, 4-pass depth sort (+hist, offsets),
+        # emission (offsets, expansion), tile sort (+hist, offsets), bins,
+        # raster fwd (+ loss), raster bwd, project bwd
+        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 1 + 1
         self.passes = tile_passes
 
     def launches_per_step(self):
@@ -170,15 +170,15 @@ class OursStep:
         contributing (tile, Gaussian) pair I_c, counted by splat_count_pairs
         (`pairs`, when taken); raster forward: 40 B per intersection and 20 B
         per pixel, plus the fused L2 loss (target in, v_img out: 24 B per
-        pixel); the sort stage includes the packing pass that runs beside it
-        (36 B in + 48 B out per Gaussian)."""
+        pixel); the projection also writes the packed records (16 B more in,
+        48 B more out per Gaussian)."""
         n, I = self.sc.spec.num_points, self.count
         h, w = self.sc.spec.img_shape
         P = h * w
         ic = (getattr(self, "pairs", None) or {}).get("tile_gaussian_contributing", 0)
         return {"raster_bwd": 52 * I + 32 * P + 36 * ic, "raster_fwd": 40 * I + 44 * P,
-                "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes + 84 * n,
-                "project_fwd": 100 * n, "project_bwd": 140 * n}
+                "sort": 16 * n * 4 + 28 * n + 8 * I + 16 * I * self.passes,
+                "project_fwd": 164 * n, "project_bwd": 140 * n}
 
     def ncu_traffic(self, kernel):
         """Measured DRAM bytes of one launch (ncu), for the 1080p scene only."""
@@ -263,7 +263,7 @@ class BatchStep:
     views in one pass of each kernel (jaxsplat_gb300.BatchSession), one CUDA
     graph per step."""
 
-    STAGES = ["project_fwd", "sort", "raster_fwd", "l2_loss", "raster_bwd", "project_bwd", "end"]
+    STAGES = OursStep.STAGES
 
     def __init__(self, seed, dev, graph=True, autotune=False, log=None, points=None):
         import torch
@@ -293,8 +293,9 @@ class BatchStep:
         tile_passes = (max(1, (int(b.num_tiles) - 1).bit_length()) + 7) // 8
         # project, depth keys, 4-pass depth sort (+hist, offsets), emission
         # (2), tile sort (+hist, offsets), bins, tile costs, 3-pass cost sort
-        # (+hist, offsets), pack, raster fwd, loss, raster bwd, project bwd
-        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 5 + 1 + 1 + 1 + 1 + 1
+        # (+hist, offsets), raster fwd (+ loss), raster bwd, project bwd; the
+        # projection writes the packed records
+        self.kernels_per_step = 1 + 1 + 6 + 2 + (2 + tile_passes) + 1 + 1 + 5 + 1 + 1 + 1
         self.passes = tile_passes
 
     def launches_per_step(self):
@@ -305,9 +306,9 @@ class BatchStep:
         atomics term (no pair count for batches: a lower bound)."""
         b, I = self.sess.batch, self.count
         E, P = int(b.num_entries), int(b.num_pixels)
-        return {"raster_bwd": 52 * I + 32 * P, "raster_fwd": 40 * I + 20 * P + 84 * E,
+        return {"raster_bwd": 52 * I + 32 * P, "raster_fwd": 40 * I + 44 * P,
                 "sort": 16 * E * 4 + 28 * E + 8 * I + 16 * I * self.passes,
-                "project_fwd": 100 * E, "project_bwd": 140 * E, "l2_loss": 36 * P}
+                "project_fwd": 164 * E, "project_bwd": 140 * E}
 
     def ncu_traffic(self, kernel):
         """DRAM bytes of one launch scaled from the quarter-size capture: the

@@ -370,6 +370,17 @@ SPLAT_API int splat_batch_project_fwd(const splat_batch *b, const float *means3d
                                       float *compensation, int64_t *total_dev,
                                       splat_stream_t stream);
 
+/* splat_batch_project_fwd that also writes every entry's packed record
+ * (splat_batch_pack's output, bit-identical), so that no packing pass runs.
+ *   colors (G,3) opacities (G,1) -> packed (E,12), 16-byte aligned */
+SPLAT_API int splat_batch_project_fwd_packed(const splat_batch *b, const float *means3d,
+                                             const float *scales, const float *quats,
+                                             const float *colors, const float *opacities,
+                                             float *cov3d, float *xys, float *depths,
+                                             int32_t *radii, float *conics, float *compensation,
+                                             int64_t *total_dev, float *packed,
+                                             splat_stream_t stream);
+
 /* Sort and bin over all views, plus the order in which the rasterizers'
  * persistent blocks take tiles (longest tile list first).  capacity and
  * count_dev as for splat_sort_and_bin with a device count.
@@ -410,6 +421,17 @@ SPLAT_API int splat_batch_rasterize_bwd(const splat_batch *b, int64_t capacity,
                                         float *v_opacity, float *v_xy, float *v_conic,
                                         uint32_t chunk, int32_t *work_counter,
                                         splat_stream_t stream);
+
+/* splat_batch_rasterize_fwd with splat_batch_l2_loss fused into its epilogue
+ * (v_img bit-identical; loss_out summed per tile). */
+SPLAT_API int splat_batch_rasterize_fwd_l2(const splat_batch *b, int64_t capacity,
+                                           const int64_t *count_dev,
+                                           const int32_t *gaussian_ids_sorted,
+                                           const int32_t *tile_bins, const int32_t *tile_order,
+                                           const float *packed, const float *target,
+                                           float *final_Ts, int32_t *final_idx, float *out_img,
+                                           float *v_img, float *loss_out, uint32_t chunk,
+                                           int32_t *work_counter, splat_stream_t stream);
 
 /* Sum over views of mean((img - target)^2) and its cotangent, per view
  * v_img = 2 (img - target) / (3 H W).  loss_out is overwritten. */

@@ -104,11 +104,14 @@ _SIGS = [
     ("splat_batch_layout", C.c_int, [C.POINTER(SplatBatch), C.POINTER(SplatView),
                                      C.POINTER(C.c_uint32)]),
     ("splat_batch_project_fwd", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 10 + [_v]),
+    ("splat_batch_project_fwd_packed", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 13 + [_v]),
     ("splat_batch_sort_workspace_size", C.c_size_t, [C.POINTER(SplatBatch), C.c_int64]),
     ("splat_batch_sort_and_bin", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 7
      + [_v, C.c_size_t, _v]),
     ("splat_batch_pack", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 5 + [_v]),
     ("splat_batch_rasterize_fwd", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 8
+     + [C.c_uint32, _v, _v]),
+    ("splat_batch_rasterize_fwd_l2", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 11
      + [C.c_uint32, _v, _v]),
     ("splat_batch_rasterize_bwd", C.c_int, [C.POINTER(SplatBatch), C.c_int64] + [_v] * 13
      + [C.c_uint32, _v, _v]),

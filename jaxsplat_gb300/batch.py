@@ -175,37 +175,58 @@ class BatchSession:
     def _stream(self):
         return C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
 
-    def _project(self):
+    def _project(self, pack=False):
         P = self._p
+        if pack:  # the packed records too (no separate packing pass)
+            _lib.check(self.lib.splat_batch_project_fwd_packed(
+                C.byref(self.batch), P(self.means3d), P(self.scales), P(self.quats),
+                P(self.colors), P(self.opacities), P(self.cov3d), P(self.xys), P(self.depths),
+                P(self.radii), P(self.conics), P(self.comp), P(self.total), P(self.packed),
+                self._stream()), "batch_project_fwd_packed")
+            return
         _lib.check(self.lib.splat_batch_project_fwd(
             C.byref(self.batch), P(self.means3d), P(self.scales), P(self.quats), P(self.cov3d),
             P(self.xys), P(self.depths), P(self.radii), P(self.conics), P(self.comp),
             P(self.total), self._stream()), "batch_project_fwd")
 
-    def step(self, mark=None):
-        """Enqueue one forward+backward of every view (no host sync)."""
+    def step(self, mark=None, side=None):
+        """Enqueue one forward+backward of every view (no host sync).  The
+        projection writes the packed records too; with ``side`` (a stream on
+        which colours, opacities and targets are still arriving, see step_io)
+        the packing pass instead runs on it once they and the projection are
+        done.  The forward rasterizer computes the per-view L2 loss in its
+        epilogue."""
         if self.capacity is None:
             self.measure_capacity()
-        P, b, s, cap, lib = self._p, C.byref(self.batch), self._stream(), self.capacity, self.lib
+        P, b, cap, lib = self._p, C.byref(self.batch), self.capacity, self.lib
+        cur = torch.cuda.current_stream(self.dev)
+        s = C.c_void_p(cur.cuda_stream)
         mark = mark or (lambda name: None)
         chk = _lib.check
         mark("project_fwd")
-        self._project()
+        self._project(pack=side is None)
+        if side is not None:
+            projected = torch.cuda.Event()
+            projected.record(cur)
+            side.wait_event(projected)
+            with torch.cuda.stream(side):
+                chk(lib.splat_batch_pack(b, P(self.xys), P(self.conics), P(self.colors),
+                                         P(self.opacities), P(self.packed),
+                                         C.c_void_p(side.cuda_stream)), "batch_pack")
         mark("sort")
         chk(lib.splat_batch_sort_and_bin(b, cap, P(self.total), P(self.xys), P(self.depths),
                                          P(self.radii), P(self.ids_sorted), P(self.tile_bins),
                                          P(self.tile_order), P(self.sort_ws),
                                          self.sort_ws.numel(), s), "batch_sort_and_bin")
+        if side is not None:
+            cur.wait_stream(side)
         mark("raster_fwd")
-        chk(lib.splat_batch_pack(b, P(self.xys), P(self.conics), P(self.colors),
-                                 P(self.opacities), P(self.packed), s), "batch_pack")
-        chk(lib.splat_batch_rasterize_fwd(b, cap, P(self.total), P(self.ids_sorted),
-                                          P(self.tile_bins), P(self.tile_order), P(self.packed),
-                                          P(self.final_Ts), P(self.final_idx), P(self.img),
-                                          self.chunk, P(self.counter), s), "batch_rasterize_fwd")
-        mark("l2_loss")
-        chk(lib.splat_batch_l2_loss(b, P(self.img), P(self.target), P(self.loss), P(self.v_img),
-                                    s), "batch_l2_loss")
+        chk(lib.splat_batch_rasterize_fwd_l2(b, cap, P(self.total), P(self.ids_sorted),
+                                             P(self.tile_bins), P(self.tile_order),
+                                             P(self.packed), P(self.target), P(self.final_Ts),
+                                             P(self.final_idx), P(self.img), P(self.v_img),
+                                             P(self.loss), self.chunk, P(self.counter), s),
+            "batch_rasterize_fwd_l2")
         mark("raster_bwd")
         chk(lib.splat_batch_rasterize_bwd(b, cap, P(self.total), P(self.ids_sorted),
                                           P(self.tile_bins), P(self.tile_order), P(self.packed),
@@ -240,14 +261,12 @@ class BatchSession:
             self.inputs[a_in:].copy_(host_in[a_in:], non_blocking=True)
 
         def mark(name):
-            if name == "raster_fwd":
-                cur.wait_stream(side)
-            elif name == "project_bwd":
+            if name == "project_bwd":
                 side.wait_stream(cur)
                 with torch.cuda.stream(side):
                     host_out[:a_out].copy_(self.outputs[:a_out], non_blocking=True)
 
-        self.step(mark=mark)
+        self.step(mark=mark, side=side)
         host_out[a_out:].copy_(self.outputs[a_out:], non_blocking=True)
         cur.wait_stream(side)
 

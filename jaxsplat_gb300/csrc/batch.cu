@@ -26,6 +26,10 @@ struct BatchProjArgs {
     float *cov3d, *xys, *depths, *conics, *comp;
     int32_t *radii;
     unsigned long long *total;
+    // optional (rec non-null): each entry's packed record, as
+    // splat_batch_pack writes it (colour and opacity of the scene Gaussian)
+    const float *colors, *opac;
+    float4 *rec;
 };
 
 __device__ __forceinline__ ProjCam view_cam(const splat_view &v, float glob, float clip,
@@ -87,6 +91,19 @@ __global__ void __launch_bounds__(kBatchBlock) batch_project_fwd_kernel(BatchPro
         a.conics[3 * i + 1] = o.conic.y;
         a.conics[3 * i + 2] = o.conic.z;
         a.comp[i] = o.comp;
+        if (a.rec) {
+            float4 *r = a.rec + 3 * i;
+            if (k < s_npts) {
+                const size_t g = (size_t)s_gbase + k;
+                write_record(r, o.center, o.conic, a.opac[g],
+                             make_float3(a.colors[3 * g], a.colors[3 * g + 1], a.colors[3 * g + 2]),
+                             __int_as_float((int)g));
+            } else {  // padding: a record that no pixel passes (pack_batch_kernel's)
+                r[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                r[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                r[2] = make_float4(0.f, -CUDART_INF_F, -CUDART_INF_F, __int_as_float((int)s_gbase));
+            }
+        }
     }
     // block total of the tile counts -> one atomic per block
     unsigned w = hits;
@@ -172,8 +189,8 @@ int launch_batch_sort_and_bin(const splat_batch &, Count, const float *, const f
 int launch_batch_pack(const splat_batch &, const float *, const float *, const float *,
                       const float *, float *, cudaStream_t);
 int launch_batch_raster_fwd(const splat_batch &, Count, const int32_t *, const int2 *,
-                            const int32_t *, const float *, float *, int32_t *, float *, int,
-                            int *, cudaStream_t);
+                            const int32_t *, const float *, float *, int32_t *, float *,
+                            const float *, float *, float *, int, int *, cudaStream_t);
 int launch_batch_raster_bwd(const splat_batch &, Count, const int32_t *, const int2 *,
                             const int32_t *, const float *, const float *, const int32_t *,
                             const float *, const float *, float *, float *, float *, float *, int,
@@ -250,10 +267,13 @@ int splat_batch_layout(splat_batch *b, splat_view *views, const uint32_t *scene_
     return SPLAT_OK;
 }
 
-int splat_batch_project_fwd(const splat_batch *b, const float *means3d, const float *scales,
-                            const float *quats, float *cov3d, float *xys, float *depths,
-                            int32_t *radii, float *conics, float *compensation,
-                            int64_t *total_dev, splat_stream_t stream) {
+}  // extern "C"
+
+static int batch_project_entry(const splat_batch *b, const float *means3d, const float *scales,
+                               const float *quats, const float *colors, const float *opacities,
+                               float *cov3d, float *xys, float *depths, int32_t *radii,
+                               float *conics, float *compensation, int64_t *total_dev,
+                               float *packed, splat_stream_t stream) {
     if (int rc = check_batch(b)) return rc;
     NEED(total_dev);
     cudaStream_t s = (cudaStream_t)stream;
@@ -273,8 +293,34 @@ int splat_batch_project_fwd(const splat_batch *b, const float *means3d, const fl
     a.cov3d = cov3d; a.xys = xys; a.depths = depths; a.conics = conics; a.comp = compensation;
     a.radii = radii;
     a.total = reinterpret_cast<unsigned long long *>(total_dev);
+    a.colors = colors; a.opac = opacities; a.rec = reinterpret_cast<float4 *>(packed);
     batch_project_fwd_kernel<<<(unsigned)(b->num_entries / kBatchBlock), kBatchBlock, 0, s>>>(a);
     return check_launch("batch_project_fwd_kernel");
+}
+
+extern "C" {
+
+int splat_batch_project_fwd(const splat_batch *b, const float *means3d, const float *scales,
+                            const float *quats, float *cov3d, float *xys, float *depths,
+                            int32_t *radii, float *conics, float *compensation,
+                            int64_t *total_dev, splat_stream_t stream) {
+    return batch_project_entry(b, means3d, scales, quats, nullptr, nullptr, cov3d, xys, depths,
+                               radii, conics, compensation, total_dev, nullptr, stream);
+}
+
+int splat_batch_project_fwd_packed(const splat_batch *b, const float *means3d,
+                                   const float *scales, const float *quats, const float *colors,
+                                   const float *opacities, float *cov3d, float *xys,
+                                   float *depths, int32_t *radii, float *conics,
+                                   float *compensation, int64_t *total_dev, float *packed,
+                                   splat_stream_t stream) {
+    if (b && b->num_entries > 0) {
+        NEED(colors); NEED(opacities); NEED(packed);
+        if (reinterpret_cast<uintptr_t>(packed) % 16)
+            return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
+    }
+    return batch_project_entry(b, means3d, scales, quats, colors, opacities, cov3d, xys, depths,
+                               radii, conics, compensation, total_dev, packed, stream);
 }
 
 size_t splat_batch_sort_workspace_size(const splat_batch *b, int64_t capacity) {
@@ -321,8 +367,28 @@ int splat_batch_rasterize_fwd(const splat_batch *b, int64_t capacity, const int6
     const Count c{reinterpret_cast<const long long *>(count_dev), 0, capacity};
     return launch_batch_raster_fwd(*b, c, gaussian_ids_sorted,
                                    reinterpret_cast<const int2 *>(tile_bins), tile_order, packed,
-                                   final_Ts, final_idx, out_img, (int)chunk, work_counter,
-                                   (cudaStream_t)stream);
+                                   final_Ts, final_idx, out_img, nullptr, nullptr, nullptr,
+                                   (int)chunk, work_counter, (cudaStream_t)stream);
+}
+
+int splat_batch_rasterize_fwd_l2(const splat_batch *b, int64_t capacity, const int64_t *count_dev,
+                                 const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
+                                 const int32_t *tile_order, const float *packed,
+                                 const float *target, float *final_Ts, int32_t *final_idx,
+                                 float *out_img, float *v_img, float *loss_out, uint32_t chunk,
+                                 int32_t *work_counter, splat_stream_t stream) {
+    if (int rc = check_batch(b)) return rc;
+    if (int rc = check_capacity(capacity)) return rc;
+    NEED(count_dev); NEED(tile_bins); NEED(tile_order); NEED(packed); NEED(target);
+    NEED(final_Ts); NEED(final_idx); NEED(out_img); NEED(v_img); NEED(loss_out);
+    NEED(work_counter);
+    if (capacity > 0) NEED(gaussian_ids_sorted);
+    if (chunk < 1 || chunk > 64) return fail(SPLAT_ERR_INVALID_ARG, "chunk must be in [1, 64]");
+    const Count c{reinterpret_cast<const long long *>(count_dev), 0, capacity};
+    return launch_batch_raster_fwd(*b, c, gaussian_ids_sorted,
+                                   reinterpret_cast<const int2 *>(tile_bins), tile_order, packed,
+                                   final_Ts, final_idx, out_img, target, v_img, loss_out,
+                                   (int)chunk, work_counter, (cudaStream_t)stream);
 }
 
 int splat_batch_rasterize_bwd(const splat_batch *b, int64_t capacity, const int64_t *count_dev,

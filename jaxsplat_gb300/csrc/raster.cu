@@ -202,21 +202,23 @@ struct RasterFwdArgs {
     float *img;
     // kLoss: the L2 loss against `target` (same layout as img), as
     // splat_l2_loss computes it: v_img = 2 (img - target) / count, and the
-    // tile's share of mean((img - target)^2) added to *loss
+    // tile's share of mean((img - target)^2) added to *loss.  Batched views:
+    // count is the tile's view's 3 W H (splat_batch_l2_loss's per-view means,
+    // summed), inv_count unused.
     const float *target;
     float *v_img, *loss;
     float inv_count;
 };
 
 // The L2 loss terms of one pixel (inside the image); returns its squared error.
-__device__ __forceinline__ float pixel_l2(const RasterFwdArgs &a, size_t pix, float r, float g,
-                                          float b) {
+__device__ __forceinline__ float pixel_l2(const RasterFwdArgs &a, size_t pix, float inv, float r,
+                                          float g, float b) {
     const float v[3] = {r, g, b};
     float sq = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float d = v[k] - a.target[3 * pix + k];
-        a.v_img[3 * pix + k] = 2.f * d * a.inv_count;
+        a.v_img[3 * pix + k] = 2.f * d * inv;
         sq += d * d;
     }
     return sq;
@@ -224,7 +226,8 @@ __device__ __forceinline__ float pixel_l2(const RasterFwdArgs &a, size_t pix, fl
 
 // Block sum of the squared errors, one atomic per tile.  Warp 0 sums the
 // staged values (a block of fewer than 32 threads: thread 0 alone).
-__device__ __forceinline__ void tile_l2_sum(const RasterFwdArgs &a, float sq, int bsize) {
+__device__ __forceinline__ void tile_l2_sum(const RasterFwdArgs &a, float sq, float inv,
+                                            int bsize) {
     __shared__ float s_sq[kMaxTile];
     const int tr = threadIdx.x;
     s_sq[tr] = sq;
@@ -235,16 +238,16 @@ __device__ __forceinline__ void tile_l2_sum(const RasterFwdArgs &a, float sq, in
             for (int k = tr; k < bsize; k += 32) t += s_sq[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (tr == 0) atomicAdd(a.loss, t * a.inv_count);
+            if (tr == 0) atomicAdd(a.loss, t * inv);
         }
     } else if (tr == 0) {
         float t = 0.f;
         for (int k = 0; k < bsize; ++k) t += s_sq[k];
-        atomicAdd(a.loss, t * a.inv_count);
+        atomicAdd(a.loss, t * inv);
     }
 }
 
-template <bool k8x4, bool kLoss = false>
+template <bool k8x4, bool kLoss = false, bool kViewLoss = false>
 __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &c) {
     __shared__ float4 s_r0[kMaxTile];
     __shared__ float4 s_r1[kMaxTile];
@@ -268,6 +271,9 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
     const size_t pix = c.pix_base + (size_t)i * c.width + j;
     const float3 bg = c.bg;
 
+    // the loss's 1 / count: the image's, or (batched views) the tile's view's,
+    // formed as splat_batch_l2_loss forms it
+    const float inv = kViewLoss ? 1.f / (3.f * (float)c.width * (float)c.height) : a.inv_count;
     if (a.count.get() == 0) {  // lib/ops.cu:119-127: background image, zero T and index
         float sq = 0.f;
         if (inside) {
@@ -276,9 +282,9 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
             a.img[3 * pix] = bg.x;
             a.img[3 * pix + 1] = bg.y;
             a.img[3 * pix + 2] = bg.z;
-            if (kLoss) sq = pixel_l2(a, pix, bg.x, bg.y, bg.z);
+            if (kLoss) sq = pixel_l2(a, pix, inv, bg.x, bg.y, bg.z);
         }
-        if (kLoss) tile_l2_sum(a, sq, bsize);
+        if (kLoss) tile_l2_sum(a, sq, inv, bsize);
         return;
     }
     if (tr < nwarps) s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
@@ -337,9 +343,9 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
         a.img[3 * pix] = r;
         a.img[3 * pix + 1] = g;
         a.img[3 * pix + 2] = b;
-        if (kLoss) sq = pixel_l2(a, pix, r, g, b);
+        if (kLoss) sq = pixel_l2(a, pix, inv, r, g, b);
     }
-    if (kLoss) tile_l2_sum(a, sq, bsize);
+    if (kLoss) tile_l2_sum(a, sq, inv, bsize);
 }
 
 template <bool k8x4, bool kLoss>
@@ -811,9 +817,9 @@ __device__ __forceinline__ void for_each_work_tile(const BatchTiles &b, unsigned
     }
 }
 
-template <bool k8x4>
+template <bool k8x4, bool kLoss>
 __global__ void __launch_bounds__(kMaxTile) raster_fwd_batch_kernel(RasterFwdArgs a, BatchTiles b) {
-    for_each_work_tile(b, a.bw, [&](const TileCtx &c) { fwd_tile<k8x4>(a, c); });
+    for_each_work_tile(b, a.bw, [&](const TileCtx &c) { fwd_tile<k8x4, kLoss, kLoss>(a, c); });
 }
 
 __global__ void __launch_bounds__(kMaxTile) raster_bwd_batch_kernel(RasterBwdArgs a, BatchTiles b) {
@@ -873,10 +879,14 @@ static BatchTiles batch_tiles(const splat_batch &b, const int32_t *order, int ch
     return t;
 }
 
+// target / v_img / loss non-null: the per-view L2 loss is fused in.
 int launch_batch_raster_fwd(const splat_batch &b, Count count, const int32_t *ids,
                             const int2 *bins, const int32_t *order, const float *rec,
-                            float *final_Ts, int32_t *final_idx, float *img, int chunk, int *next,
-                            cudaStream_t s) {
+                            float *final_Ts, int32_t *final_idx, float *img, const float *target,
+                            float *v_img, float *loss, int chunk, int *next, cudaStream_t s) {
+    const bool fused = target != nullptr;
+    if (fused && cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess)
+        return check_launch("loss memset");
     if (b.num_tiles == 0) return SPLAT_OK;
     if (cudaMemsetAsync(next, 0, sizeof(int), s) != cudaSuccess)
         return check_launch("work counter memset");
@@ -886,18 +896,20 @@ int launch_batch_raster_fwd(const splat_batch &b, Count count, const int32_t *id
     a.count = count; a.ids = ids; a.bins = bins;
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = nullptr;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
-    a.target = nullptr; a.v_img = nullptr; a.loss = nullptr; a.inv_count = 0.f;
+    a.target = target; a.v_img = v_img; a.loss = loss; a.inv_count = 0.f;
     const BatchTiles t = batch_tiles(b, order, chunk, next);
     const int threads = (int)(b.block_width * b.block_width);
     int grid = 0;
-    if (b.block_width == 16) {
-        if (int rc = persistent_grid(raster_fwd_batch_kernel<true>, threads, &grid)) return rc;
-        raster_fwd_batch_kernel<true><<<grid, threads, 0, s>>>(a, t);
-    } else {
-        if (int rc = persistent_grid(raster_fwd_batch_kernel<false>, threads, &grid)) return rc;
-        raster_fwd_batch_kernel<false><<<grid, threads, 0, s>>>(a, t);
-    }
-    return check_launch("raster_fwd_batch_kernel");
+    auto run = [&](auto kernel) -> int {
+        if (int rc = persistent_grid(kernel, threads, &grid)) return rc;
+        kernel<<<grid, threads, 0, s>>>(a, t);
+        return check_launch("raster_fwd_batch_kernel");
+    };
+    if (b.block_width == 16)
+        return fused ? run(raster_fwd_batch_kernel<true, true>)
+                     : run(raster_fwd_batch_kernel<true, false>);
+    return fused ? run(raster_fwd_batch_kernel<false, true>)
+                 : run(raster_fwd_batch_kernel<false, false>);
 }
 
 int launch_batch_raster_bwd(const splat_batch &b, Count count, const int32_t *ids,

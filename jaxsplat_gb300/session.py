@@ -158,8 +158,16 @@ class RenderSession:
     def _check(self, rc, what):
         _lib.check(rc, what)
 
-    def _project(self):
+    def _project(self, pack=False):
         P, pr = self._p, C.byref(self.params)
+        if pack:  # the packed records too (no separate packing pass)
+            self._check(self.lib.splat_project_fwd_packed(
+                pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat),
+                P(self.colors), P(self.opacities), P(self.cov3d), P(self.xys), P(self.depths),
+                P(self.radii), P(self.conics), P(self.comp), P(self.ntiles), P(self.cum),
+                P(self.total), P(self.packed), P(self.proj_ws), self.proj_ws.numel(),
+                self._stream()), "project_fwd_packed")
+            return
         self._check(self.lib.splat_project_fwd(
             pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat), P(self.cov3d),
             P(self.xys), P(self.depths), P(self.radii), P(self.conics), P(self.comp),
@@ -169,8 +177,10 @@ class RenderSession:
     def step(self, mark=None, side=None):
         """Enqueue one forward+backward on the current stream (no host sync).
         ``mark(stage)`` is called before each stage and with "end" after the
-        last (e.g. to record CUDA events).  The packing pass runs on a second
-        stream (``side``, or the session's own) while the sort runs; the
+        last (e.g. to record CUDA events).  The projection writes the packed
+        records too; with ``side`` (a stream on which the colours, opacities,
+        background and target are still arriving, see step_io) the packing
+        pass instead runs on it once they and the projection are done.  The
         forward rasterizer computes the L2 loss in its epilogue."""
         if self.capacity is None:
             self.measure_capacity()
@@ -178,25 +188,24 @@ class RenderSession:
         lib = self.lib
         cur = torch.cuda.current_stream(self.dev)
         s = C.c_void_p(cur.cuda_stream)
-        if side is None:
-            side = self._pack_stream = (getattr(self, "_pack_stream", None)
-                                        or torch.cuda.Stream(self.dev))
         mark = mark or (lambda name: None)
         mark("project_fwd")
-        self._project()
-        projected = torch.cuda.Event()
-        projected.record(cur)
-        side.wait_event(projected)
-        with torch.cuda.stream(side):
-            self._check(lib.splat_pack_splats(
-                pr, P(self.xys), P(self.conics), P(self.colors), P(self.opacities),
-                P(self.packed), C.c_void_p(side.cuda_stream)), "pack_splats")
+        self._project(pack=side is None)
+        if side is not None:
+            projected = torch.cuda.Event()
+            projected.record(cur)
+            side.wait_event(projected)
+            with torch.cuda.stream(side):
+                self._check(lib.splat_pack_splats(
+                    pr, P(self.xys), P(self.conics), P(self.colors), P(self.opacities),
+                    P(self.packed), C.c_void_p(side.cuda_stream)), "pack_splats")
         mark("sort")
         self._check(lib.splat_sort_and_bin(
             pr, cap, P(self.total), P(self.xys), P(self.depths), P(self.radii), P(self.cum),
             P(self.ids_sorted), P(self.tile_bins), None, None, None, P(self.sort_ws),
             self.sort_ws.numel(), s), "sort_and_bin")
-        cur.wait_stream(side)
+        if side is not None:
+            cur.wait_stream(side)
         mark("raster_fwd")
         self._check(lib.splat_rasterize_fwd_l2(
             pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),

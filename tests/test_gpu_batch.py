@@ -56,6 +56,10 @@ def test_batch_views_match_single_view_renders(bw):
         Ts, idx = bs.view_final(k)
         torch.testing.assert_close(bs.view_image(k), s.img, rtol=0, atol=0)
         torch.testing.assert_close(Ts, s.final_Ts, rtol=0, atol=0)
+        # the loss cotangent from the fused epilogue, per view
+        b0, h, w = bs._pix(k)
+        torch.testing.assert_close(bs.v_img[b0:b0 + h * w].reshape(h, w, 3), s.v_img, rtol=0,
+                                   atol=0)
         # final_idx indexes the batch's list: the view's own index plus the
         # intersections of the views before it, for pixels with a contributor
         off = int(lengths[:bs.views_host[k].tile_base].sum())

@@ -77,3 +77,32 @@ def test_fused_forward_loss_without_intersections():
     loss, v_img = _ops.l2_loss(f["img"], target)
     assert torch.equal(v_img, f["v_img"])
     assert abs(float(f["loss"]) - float(loss)) <= 1e-6 * float(loss)
+
+
+def test_fused_batch_projection_matches_projection_and_pack():
+    """splat_batch_project_fwd_packed = splat_batch_project_fwd +
+    splat_batch_pack, padding entries included, bit for bit."""
+    import torch
+
+    from jaxsplat_gb300.batch import BatchSession
+    from jaxsplat_gb300.scenes import make_batch
+
+    scenes, views, targets = make_batch(4, scene_points=(1500, 2600), views_per_scene=2,
+                                        sizes=((40, 56), (72, 48)))
+    bs = BatchSession(scenes, views, targets, block_size=16)
+    bs._project(pack=False)
+    import ctypes
+
+    rc = bs.lib.splat_batch_pack(ctypes.byref(bs.batch),
+                                 *(bs._p(t) for t in (bs.xys, bs.conics, bs.colors,
+                                                      bs.opacities, bs.packed)), bs._stream())
+    assert rc == 0
+    ref = {k: getattr(bs, k).clone() for k in ("packed", "xys", "conics", "cov3d", "depths",
+                                                "radii", "comp", "total")}
+    for k in ("packed", "xys", "conics"):
+        getattr(bs, k).fill_(-7.0)
+    bs._project(pack=True)
+    for k, v in ref.items():
+        assert torch.equal(v.view(torch.int32) if v.is_floating_point() else v,
+                           getattr(bs, k).view(torch.int32) if v.is_floating_point()
+                           else getattr(bs, k)), k
