@@ -50,6 +50,11 @@ NCU_TRAFFIC = {"raster_bwd": 104_166_400 + 4_871_168}
 NCU_BATCH_QUARTER = {"raster_bwd": (1_278_222_080, 106_604_800, 23_673_320)}
 
 
+def radix_passes(bits: int) -> int:
+    """Onesweep passes over `bits` key bits (8 per pass)."""
+    return (max(1, bits) + 7) // 8
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -154,7 +159,7 @@ class OursStep:
         h, w = kw["img_shape"]
         bw = sc.spec.block_width
         tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
-        tile_passes = (max(1, (tiles - 1).bit_length()) + 7) // 8
+        tile_passes = radix_passes(max(1, (tiles - 1).bit_length()))
         # project (+ packing), depth keys, 4-pass depth sort (+hist, offsets),
         # emission (offsets, expansion), tile sort (+hist, offsets), bins,
         # raster fwd (+ loss), raster bwd, project bwd
@@ -290,7 +295,7 @@ class BatchStep:
             s.capture()
             s.capture_io(self.host_in, self.host_out)
         b = s.batch
-        tile_passes = (max(1, (int(b.num_tiles) - 1).bit_length()) + 7) // 8
+        tile_passes = radix_passes(max(1, (int(b.num_tiles) - 1).bit_length()))
         # project, depth keys, 4-pass depth sort (+hist, offsets), emission
         # (2), tile sort (+hist, offsets), bins, tile costs, 3-pass cost sort
         # (+hist, offsets), raster fwd (+ loss), raster bwd, project bwd; the

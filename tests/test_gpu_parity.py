@@ -153,6 +153,31 @@ def test_cuda_matches_oracle_edge_shapes(bw, shape):
         assert normwise_rel(out[k], ref[k]) <= GRAD_RTOL, k
 
 
+@pytest.mark.parametrize("bw,shape", [(16, (320, 400)), (2, (600, 800))])
+def test_cuda_matches_oracle_tile_ids_one_bit_past_a_byte(bw, shape):
+    """Tile ids of 9 bits (500 tiles) and of 17 bits (120,000 tiles): a last
+    radix pass over a single bit sorts like the reference."""
+    from gpu_pipeline import run_cuda
+    from jaxsplat_gb300.scenes import make_scene
+    from oracle.oracle import Oracle
+
+    h, w = shape
+    tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
+    bits = (tiles - 1).bit_length()
+    assert bits % 8 == 1
+    sc = make_scene("small", seed=17 + bw, num_points=3000, img_shape=shape)
+    inp = dict(means3d=sc.means3d, scales=sc.scales, quats=sc.quats, colors=sc.colors,
+               opacities=sc.opacities, viewmat=sc.viewmat,
+               background=np.asarray([0.3, 0.1, 0.7], np.float32))
+    kw = sc.kwargs
+    ref = _oracle_case(Oracle("f32"), inp, kw, bw)
+    out = run_cuda(inp, kw, bw)
+    assert int(out["count"]) > 2 * 4096  # several sort partitions
+    for k in ("isect_ids", "gaussian_ids_sorted", "tile_bins", "final_idx"):
+        np.testing.assert_array_equal(out[k], ref[k], err_msg=k)
+    assert np.abs(out["img"] - ref["img"]).max() <= IMG_ATOL
+
+
 def test_all_culled_renders_background():
     """No intersections (lib/ops.cu:119-127): image = background, final_Ts =
     final_idx = 0, zero gradients."""
