@@ -453,6 +453,28 @@ def time_stages(st, steps, flush):
     return {k: v / steps for k, v in stages.items()}
 
 
+def link_bandwidth(dev, nbytes=256 << 20, reps=3):
+    """Host link bandwidth of this machine, GB/s: one pinned 256 MB copy each
+    way, best of `reps` (measured outside the timed regions; it bounds e2e)."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = round(nbytes / (best * 1e-3) / 1e9, 1)
+    return out
+
+
 def time_e2e(st, steps, flush):
     """Host buffers: H2D of the inputs and D2H of loss + gradients inside.
     Steps with `download()` move their outputs as one block; the others copy
@@ -720,7 +742,7 @@ def main_batch(a, torch, world, rank, local, dist, dev):
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": config,
             "e2e": {"value": round(e2e_ms / world, 4), "unit": UNIT, "h2d_bytes_per_step": bi,
-                    "d2h_bytes_per_step": bo},
+                    "d2h_bytes_per_step": bo, "link_gbs": link_bandwidth(dev)},
             "clocks": clk.summary()}
     if a.impl == "reference":
         line["impl"] = "reference"
@@ -834,7 +856,7 @@ def main():
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, benchmark scene distributions)", "config": config,
             "e2e": {"value": round(e2e_ms / world, 4), "unit": UNIT, "h2d_bytes_per_step": bi,
-                    "d2h_bytes_per_step": bo},
+                    "d2h_bytes_per_step": bo, "link_gbs": link_bandwidth(dev)},
             "clocks": clk.summary()}
     if a.impl == "reference":
         line["impl"] = "reference"

@@ -314,25 +314,63 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
         __syncthreads();
         const int n = min(bsize, range.y - start);
         const int cnt = warp_list(s_mask, 0, n, warp, lane, wmask, s_list[warp]);
-        for (int k = 0; k < cnt && !done; ++k) {
+        // two entries per iteration: their loads and exponentials are
+        // independent, the blending stays in list order
+        int k = 0;
+        for (; k + 1 < cnt && !done; k += 2) {
+            const int t0 = s_list[warp][k], t1 = s_list[warp][k + 1];
+            const float4 p0 = s_r0[t0], q0 = s_r1[t0];
+            const float4 p1 = s_r0[t1], q1 = s_r1[t1];
+            const float sg0 = falloff(p0.z, p0.w, q0.x, p0.x - px, p0.y - py);
+            const float sg1 = falloff(p1.z, p1.w, q1.x, p1.x - px, p1.y - py);
+            const float al0 = fminf(0.999f, q0.y * __expf(-sg0));
+            const float al1 = fminf(0.999f, q1.y * __expf(-sg1));
+            if (!(sg0 < 0.f || al0 < 1.f / 255.f)) {
+                const float next_T = T * (1.f - al0);
+                if (next_T <= 1e-4f) {
+                    done = true;
+                    break;
+                }
+                const float vis = al0 * T;
+                acc.x = blend(acc.x, q0.z, vis);
+                acc.y = blend(acc.y, q0.w, vis);
+                acc.z = blend(acc.z, s_blue[t0], vis);
+                T = next_T;
+                cur_idx = start + t0;
+            }
+            if (!(sg1 < 0.f || al1 < 1.f / 255.f)) {
+                const float next_T = T * (1.f - al1);
+                if (next_T <= 1e-4f) {
+                    done = true;
+                    break;
+                }
+                const float vis = al1 * T;
+                acc.x = blend(acc.x, q1.z, vis);
+                acc.y = blend(acc.y, q1.w, vis);
+                acc.z = blend(acc.z, s_blue[t1], vis);
+                T = next_T;
+                cur_idx = start + t1;
+            }
+        }
+        if (k < cnt && !done) {
             const int t = s_list[warp][k];
             const float4 r0 = s_r0[t];
             const float4 r1 = s_r1[t];
-            const float dx = r0.x - px, dy = r0.y - py;
-            const float sigma = falloff(r0.z, r0.w, r1.x, dx, dy);
+            const float sigma = falloff(r0.z, r0.w, r1.x, r0.x - px, r0.y - py);
             const float alpha = fminf(0.999f, r1.y * __expf(-sigma));
-            if (sigma < 0.f || alpha < 1.f / 255.f) continue;
-            const float next_T = T * (1.f - alpha);
-            if (next_T <= 1e-4f) {
-                done = true;
-                break;
+            if (!(sigma < 0.f || alpha < 1.f / 255.f)) {
+                const float next_T = T * (1.f - alpha);
+                if (next_T <= 1e-4f) {
+                    done = true;
+                } else {
+                    const float vis = alpha * T;
+                    acc.x = blend(acc.x, r1.z, vis);
+                    acc.y = blend(acc.y, r1.w, vis);
+                    acc.z = blend(acc.z, s_blue[t], vis);
+                    T = next_T;
+                    cur_idx = start + t;
+                }
             }
-            const float vis = alpha * T;
-            acc.x = blend(acc.x, r1.z, vis);
-            acc.y = blend(acc.y, r1.w, vis);
-            acc.z = blend(acc.z, s_blue[t], vis);
-            T = next_T;
-            cur_idx = start + t;
         }
     }
     float sq = 0.f;
@@ -818,7 +856,7 @@ __device__ __forceinline__ void for_each_work_tile(const BatchTiles &b, unsigned
 }
 
 template <bool k8x4, bool kLoss>
-__global__ void __launch_bounds__(kMaxTile) raster_fwd_batch_kernel(RasterFwdArgs a, BatchTiles b) {
+__global__ void __launch_bounds__(kMaxTile, 5) raster_fwd_batch_kernel(RasterFwdArgs a, BatchTiles b) {
     for_each_work_tile(b, a.bw, [&](const TileCtx &c) { fwd_tile<k8x4, kLoss, kLoss>(a, c); });
 }
 
