@@ -516,6 +516,37 @@ def time_e2e(st, steps, flush):
     return total / steps, bi, bo
 
 
+def time_e2e_streamed(st, steps, flush):
+    """Consecutive steps through RenderSession.stream_step: each step's inputs
+    go host -> device and its loss and gradients device -> host, double
+    buffered so that step i+1's upload and step i's download overlap step i's
+    computation.  The L2 flush before every step runs on the compute stream,
+    inside the timed region."""
+    torch = st.torch
+    sess = st.sess
+    sess.capture_stream()
+    for _ in range(3):  # warm-up
+        flush.fill_(1)
+        sess.stream_step(st.host_in, st.host_out)
+    sess.stream_sync()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        flush.fill_(1)
+        sess.stream_step(st.host_in, st.host_out)
+    sess.stream_sync()
+    b.record()
+    torch.cuda.synchronize()
+    sess.check()
+    return {"value": round(a.elapsed_time(b) / steps, 4), "unit": UNIT,
+            "h2d_bytes_per_step": st.h2d_bytes, "d2h_bytes_per_step": st.d2h_bytes,
+            "steps": steps,
+            "mode": "RenderSession.stream_step: every step uploads its inputs and downloads its "
+                    "loss and gradients; double-buffered, so step i+1's upload and step i's "
+                    "download run while step i computes; L2 flush inside the timed region"}
+
+
 def cpu_baseline(sc):
     """The CPU restatement (oracle/, fp32, all host threads) on one step of
     the same workload."""
@@ -868,6 +899,8 @@ def main():
         st.sess.check()  # no step overflowed its capacity, no device check fired
         line["gpu_launches"] = st.launches_per_step() * a.steps
         line["cuda_graph"] = st.graph
+        if world == 1:
+            line["e2e_streamed"] = time_e2e_streamed(st, max(3, a.steps // 2), flush)
         st.pairs = st.sess.count_pairs()  # work counts of the timed step's list
         add_stages_and_roofline(line, st, a.steps, flush)
         add_compute_roofline(line, st)

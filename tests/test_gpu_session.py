@@ -115,3 +115,35 @@ def test_step_io_copies_inputs_in_and_results_out():
     assert abs(float(got[0]) - float(ref[0])) <= 1e-6 * max(1.0, abs(float(ref[0])))
     assert normwise_rel(got.numpy(), ref.numpy()) <= 1e-5
     torch.testing.assert_close(sess.target.cpu(), torch.from_numpy(target_b), rtol=0, atol=0)
+
+
+def test_stream_step_matches_step_io_for_each_input():
+    """stream_step (double-buffered, copies overlapped across steps): four
+    consecutive steps alternating two input sets each return the loss and
+    gradients that step_io gives for that input set."""
+    import torch
+
+    sc = _scene()
+    sess = _session(sc)
+    sess.measure_capacity()
+    targets = [sc.target, (sc.target * 0.5 + 0.25).astype(np.float32)]
+    scales = [sc.scales, (sc.scales * 1.1).astype(np.float32)]
+    host_in = [sess.host_inputs(sc.means3d, scales[j], sc.quats, sc.colors, sc.opacities,
+                                sc.viewmat, sc.background, targets[j]) for j in range(2)]
+    n_out = sess.outputs.numel()
+    refs = []
+    for j in range(2):
+        out = torch.empty(n_out, dtype=torch.float32, pin_memory=True)
+        sess.step_io(host_in[j], out)
+        torch.cuda.synchronize()
+        refs.append(out.clone())
+    assert float(refs[0][0]) != float(refs[1][0])
+    outs = [torch.full((n_out,), float("nan"), pin_memory=True) for _ in range(4)]
+    for i in range(4):
+        sess.stream_step(host_in[i % 2], outs[i])
+    sess.stream_sync()
+    torch.cuda.synchronize()
+    for i in range(4):
+        ref = refs[i % 2]
+        assert abs(float(outs[i][0]) - float(ref[0])) <= 1e-6 * max(1.0, abs(float(ref[0]))), i
+        assert normwise_rel(outs[i].numpy(), ref.numpy()) <= 1e-5, i
