@@ -25,22 +25,12 @@ import numpy as np
 import torch
 
 from . import _lib
+from ._buffers import block as _block
 from ._ops import _status_word
+from .streaming import StreamingSteps
 
 
-def _block(shapes, device, pin=False):
-    """One fp32 buffer holding the named shapes back to back, each starting on
-    a 256-byte boundary; returns (buffer, {name: view})."""
-    offs, total = [], 0
-    for _, shape in shapes:
-        offs.append(total)
-        total += (math.prod(shape) + 63) // 64 * 64
-    buf = torch.zeros(total, dtype=torch.float32, device=device, pin_memory=pin)
-    return buf, {name: buf[o:o + math.prod(shape)].view(shape)
-                 for (name, shape), o in zip(shapes, offs)}
-
-
-class BatchSession:
+class BatchSession(StreamingSteps):
     """scenes: list of dicts with means3d (N,3), scales (N,3), quats (N,4),
     colors (N,3), opacities (N,1).  views: list of dicts with scene (index),
     viewmat (4,4), img_shape (H, W), f (fx, fy), c (cx, cy) and optionally
@@ -62,8 +52,9 @@ class BatchSession:
         P = sum(int(v["img_shape"][0]) * int(v["img_shape"][1]) for v in self.view_specs)
         # inputs (scene arrays, targets) and outputs (loss, scene gradients) as
         # single blocks: one host transfer each way per step
-        self.inputs, views_in = _block(self.input_shapes(G, P), self.dev)
-        self.outputs, views_out = _block(self.output_shapes(G), self.dev)
+        self._io_shapes = (self.input_shapes(G, P), self.output_shapes(G))
+        self.inputs, views_in = _block(self._io_shapes[0], self.dev)
+        self.outputs, views_out = _block(self._io_shapes[1], self.dev)
         for name, t in list(views_in.items()) + list(views_out.items()):
             setattr(self, name, t)
         for k, w in (("means3d", 3), ("scales", 3), ("quats", 4), ("colors", 3), ("opacities", 1)):
@@ -76,6 +67,9 @@ class BatchSession:
             self._size(int(capacity))
 
     # -- layout and buffers ----------------------------------------------------
+    def _stream_shapes(self):
+        return self._io_shapes
+
     @staticmethod
     def input_shapes(G, P):
         return [("means3d", (G, 3)), ("scales", (G, 3)), ("quats", (G, 4)), ("colors", (G, 3)),
@@ -141,6 +135,7 @@ class BatchSession:
         self.capacity = None
         self.graph = None
         self.graph_io = None
+        self._stream_graphs = None
 
     def _size(self, capacity: int):
         self.capacity = max(int(capacity), 1)
@@ -152,6 +147,7 @@ class BatchSession:
         self.sort_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
         self.graph = None
         self.graph_io = None
+        self._stream_graphs = None
 
     def set_targets(self, targets):
         for k, t in enumerate(targets):
@@ -370,6 +366,7 @@ class BatchSession:
             for ch in chunks:
                 self.chunk = int(ch)
                 self.graph = None
+                self._stream_graphs = None
                 self.capture()
                 ms = self.time_replays(steps)
                 self.check()

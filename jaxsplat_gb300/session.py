@@ -26,22 +26,12 @@ import math
 import torch
 
 from . import _lib
+from ._buffers import block as _block
 from ._ops import _status_word
+from .streaming import StreamingSteps
 
 
-def _block(shapes, device, pin=False):
-    """One fp32 buffer holding the named shapes back to back, each starting on
-    a 256-byte boundary; returns (buffer, {name: view})."""
-    offs, total = [], 0
-    for _, shape in shapes:
-        offs.append(total)
-        total += (math.prod(shape) + 63) // 64 * 64
-    buf = torch.zeros(total, dtype=torch.float32, device=device, pin_memory=pin)
-    return buf, {name: buf[o:o + math.prod(shape)].view(shape)
-                 for (name, shape), o in zip(shapes, offs)}
-
-
-class RenderSession:
+class RenderSession(StreamingSteps):
     def __init__(self, num_points: int, *, img_shape, f, c, glob_scale: float = 1.0,
                  clip_thresh: float = 0.01, block_size: int = 16, capacity: int | None = None,
                  device="cuda"):
@@ -88,10 +78,14 @@ class RenderSession:
         self.capacity = None
         self.graph = None
         self.graph_io = None
+        self._stream_graphs = None
         if capacity is not None:
             self._size(int(capacity))
 
     # -- buffers -------------------------------------------------------------
+    def _stream_shapes(self):
+        return self.input_shapes(), self.output_shapes()
+
     def input_shapes(self):
         n, h, w = self.n, self.h, self.w
         # what the projection reads first, then what the rasterizer and the
@@ -131,6 +125,7 @@ class RenderSession:
         self.sort_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
         self.graph = None
         self.graph_io = None
+        self._stream_graphs = None
 
     def set_inputs(self, means3d, scales, quats, colors, opacities, viewmat, background, target):
         for dst, src in ((self.means3d, means3d), (self.scales, scales), (self.quats, quats),
@@ -314,83 +309,6 @@ class RenderSession:
         if self.graph is None:
             self.capture()
         self.graph.replay()
-
-    # -- streaming: consecutive steps with overlapped host copies ----------------
-    def _bind(self, k: int):
-        """Point the input and output views at block pair k."""
-        self.inputs, self.outputs = self._in_blocks[k], self._out_blocks[k]
-        for name, t in self._in_views[k].items():
-            setattr(self, name, t)
-        for name, t in self._out_views[k].items():
-            setattr(self, name, t)
-
-    def capture_stream(self):
-        """Prepare ``stream_step``: a second input block and output block, and
-        one graph of ``step()`` per block pair (the intermediate buffers are
-        shared: the steps' computations stay in order on one stream)."""
-        if self.capacity is None:
-            self.measure_capacity()
-        if getattr(self, "_stream_graphs", None) is not None:
-            return
-        views_in = {name: getattr(self, name) for name, _ in self.input_shapes()}
-        views_out = {name: getattr(self, name) for name, _ in self.output_shapes()}
-        in1, vin1 = _block(self.input_shapes(), self.dev)
-        out1, vout1 = _block(self.output_shapes(), self.dev)
-        in1.copy_(self.inputs)
-        self._in_blocks, self._out_blocks = [self.inputs, in1], [self.outputs, out1]
-        self._in_views, self._out_views = [views_in, vin1], [views_out, vout1]
-        graphs = []
-        for k in (0, 1):
-            self._bind(k)
-            side = torch.cuda.Stream(self.dev)  # warm-up outside the capture
-            side.wait_stream(torch.cuda.current_stream(self.dev))
-            with torch.cuda.stream(side):
-                self.step()
-            torch.cuda.current_stream(self.dev).wait_stream(side)
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                self.step()
-            graphs.append(g)
-        self._bind(0)
-        self._stream_graphs = graphs
-        self._copy_in = torch.cuda.Stream(self.dev)
-        self._copy_out = torch.cuda.Stream(self.dev)
-        ev = lambda: [torch.cuda.Event(), torch.cuda.Event()]
-        self._in_done, self._comp_done, self._out_done = ev(), ev(), ev()
-        self._stream_i = 0
-
-    def stream_step(self, host_in, host_out):
-        """Enqueue one step from pinned ``host_in`` (laid out like ``inputs``) to
-        pinned ``host_out`` (like ``outputs``) without waiting for the previous
-        ones: the inputs go to the block pair the step before last used, so
-        that this step's upload and the previous step's download run while the
-        previous step computes.  Step i waits for its upload and for step
-        i-2's download (which read its output block); its upload waits for
-        step i-2's computation (which read its input block).  ``stream_sync()``
-        orders the current stream after every enqueued step."""
-        if getattr(self, "_stream_graphs", None) is None:
-            self.capture_stream()
-        k = self._stream_i & 1
-        cur = torch.cuda.current_stream(self.dev)
-        cin, cout = self._copy_in, self._copy_out
-        cin.wait_event(self._comp_done[k])
-        with torch.cuda.stream(cin):
-            self._in_blocks[k].copy_(host_in, non_blocking=True)
-        self._in_done[k].record(cin)
-        cur.wait_event(self._in_done[k])
-        cur.wait_event(self._out_done[k])
-        self._stream_graphs[k].replay()
-        self._comp_done[k].record(cur)
-        cout.wait_event(self._comp_done[k])
-        with torch.cuda.stream(cout):
-            host_out.copy_(self._out_blocks[k], non_blocking=True)
-        self._out_done[k].record(cout)
-        self._stream_i += 1
-
-    def stream_sync(self):
-        """Order the current stream after every step ``stream_step`` enqueued."""
-        if getattr(self, "_stream_graphs", None) is not None:
-            torch.cuda.current_stream(self.dev).wait_stream(self._copy_out)
 
     def check(self) -> int:
         """Synchronise; raise if any step overflowed or a device check fired.

@@ -135,3 +135,33 @@ def test_batch_step_io_matches_device_step():
     ref = bs.outputs.cpu()
     assert abs(float(got[0]) - float(ref[0])) <= 1e-6 * max(1.0, abs(float(ref[0])))
     assert normwise_rel(got.numpy(), ref.numpy()) <= 1e-5
+
+
+def test_batch_stream_step_matches_step_io_for_each_input():
+    """BatchSession.stream_step: consecutive steps alternating two input
+    blocks return what step_io returns for each."""
+    import torch
+
+    bs, *_ = _batch(16, (3000, 2000), 2)
+    bs.measure_capacity()
+    host_a = bs.inputs.cpu().pin_memory()
+    host_b = host_a.clone().pin_memory()
+    tgt = bs.target.data_ptr() - bs.inputs.data_ptr()
+    host_b[tgt // 4:] *= 0.5  # the targets
+    n_out = bs.outputs.numel()
+    refs = []
+    for h in (host_a, host_b):
+        out = torch.empty(n_out, dtype=torch.float32, pin_memory=True)
+        bs.step_io(h, out)
+        torch.cuda.synchronize()
+        refs.append(out.clone())
+    assert float(refs[0][0]) != float(refs[1][0])
+    outs = [torch.full((n_out,), float("nan"), pin_memory=True) for _ in range(4)]
+    for i in range(4):
+        bs.stream_step((host_a, host_b)[i % 2], outs[i])
+    bs.stream_sync()
+    torch.cuda.synchronize()
+    for i in range(4):
+        ref = refs[i % 2]
+        assert abs(float(outs[i][0]) - float(ref[0])) <= 1e-6 * max(1.0, abs(float(ref[0]))), i
+        assert normwise_rel(outs[i].numpy(), ref.numpy()) <= 1e-5, i
