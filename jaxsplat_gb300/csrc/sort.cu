@@ -98,6 +98,35 @@ __global__ void __launch_bounds__(kRadix) radix_offsets_kernel(const unsigned *h
     offs[d * kRadix + t] = s[t] - x;
 }
 
+// Digit counts of the keys a producer kernel writes, for every pass of the
+// radix sort that follows (the sort then skips its histogram pass over the
+// keys): a block counts in shared memory and adds its nonzero counts to the
+// global histogram once.
+struct KeyHist {
+    unsigned *hist;  // [passes][kRadix] of the sort, zeroed before the producer; null: none
+    int passes;
+    int end_bit;
+};
+
+__device__ __forceinline__ void key_hist_zero(unsigned (*sh)[kRadix]) {
+    for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) (&sh[0][0])[i] = 0u;
+}
+
+__device__ __forceinline__ void key_hist_add(const KeyHist &h, unsigned (*sh)[kRadix], uint32_t k) {
+    for (int d = 0; d < h.passes; ++d) {
+        const int shift = d * kRadixBits;
+        const int bits = min(kRadixBits, h.end_bit - shift);
+        atomicAdd(&sh[d][digit_of(k, shift, (1u << bits) - 1u)], 1u);
+    }
+}
+
+__device__ __forceinline__ void key_hist_flush(const KeyHist &h, unsigned (*sh)[kRadix]) {
+    for (int i = threadIdx.x; i < h.passes * kRadix; i += blockDim.x) {
+        const unsigned c = (&sh[0][0])[i];
+        if (c) atomicAdd(&h.hist[i], c);
+    }
+}
+
 // 32-bit look-back words: [flag:2][count:30].  The count travels inside the
 // word, so the words need no ordering against other memory: relaxed loads and
 // stores at device scope are enough.
@@ -329,25 +358,40 @@ static RadixBufs radix_layout(Arena &ar, long long count, int end_bit) {
     return b;
 }
 
+// Zeroes a sort's histogram, tickets and look-back words (before a producer
+// that fills the histogram, see KeyHist).
+static int radix_clear(const RadixBufs &b, cudaStream_t s) {
+    if (cudaMemsetAsync(b.hist, 0, b.zero_bytes, s) != cudaSuccess)
+        return check_launch("sort workspace memset");
+    return SPLAT_OK;
+}
+
+static KeyHist key_hist(const RadixBufs &b, int end_bit) {
+    return KeyHist{b.hist, b.passes, end_bit};
+}
+
 // Sorts (ka, va) by the low end_bit bits of the keys.  Returns the buffers
 // holding the result; the last pass writes the values to vals_final instead
-// when it is given.
+// when it is given.  hist_ready: radix_clear ran and the producer of the keys
+// filled the histogram (KeyHist), so neither the clearing nor the histogram
+// pass runs here.
 static int radix_sort(uint32_t *status, uint32_t spin, const RadixBufs &b, Count count,
                       int end_bit, int32_t *vals_final, const uint32_t **keys_sorted,
-                      const int32_t **vals_sorted, cudaStream_t s) {
+                      const int32_t **vals_sorted, cudaStream_t s, bool hist_ready = false) {
     if (count.cap > (long long)kLbMask)
         return fail(SPLAT_ERR_OVERFLOW, "sort of %lld keys exceeds %u", count.cap, kLbMask);
     *keys_sorted = b.ka;
     *vals_sorted = b.va;
     if (count.cap == 0) return SPLAT_OK;
-    if (cudaMemsetAsync(b.hist, 0, b.zero_bytes, s) != cudaSuccess)
-        return check_launch("sort workspace memset");
-    HistArgs h{b.ka, count, b.passes, end_bit, b.hist};
-    long long blocks = (count.cap + 256 * 16 - 1) / (256 * 16);
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    if (blocks < 1) blocks = 1;
-    radix_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(h);
-    if (int rc = check_launch("radix_hist_kernel")) return rc;
+    if (!hist_ready) {
+        if (int rc = radix_clear(b, s)) return rc;
+        HistArgs h{b.ka, count, b.passes, end_bit, b.hist};
+        long long blocks = (count.cap + 256 * 16 - 1) / (256 * 16);
+        if (blocks > 152 * 8) blocks = 152 * 8;
+        if (blocks < 1) blocks = 1;
+        radix_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(h);
+        if (int rc = check_launch("radix_hist_kernel")) return rc;
+    }
     radix_offsets_kernel<<<b.passes, kRadix, 0, s>>>(b.hist, b.offs);
     if (int rc = check_launch("radix_offsets_kernel")) return rc;
     uint32_t *kin = b.ka, *kout = b.kb;
@@ -383,12 +427,26 @@ static int radix_sort(uint32_t *status, uint32_t spin, const RadixBufs &b, Count
 // ---------------------------------------------------------------------------
 // Stage 1 input: 32-bit depth keys (Gaussians that hit no tile sort last).
 
-__global__ void depth_keys_kernel(int n, const float *depths, const int32_t *radii, uint32_t *keys,
-                                  int32_t *vals) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    keys[i] = radii[i] > 0 ? __float_as_uint(depths[i]) : 0xffffffffu;
-    vals[i] = i;
+// Grid-stride, with the depth sort's digit counts (KeyHist).
+__global__ void __launch_bounds__(256) depth_keys_kernel(int n, const float *depths,
+                                                         const int32_t *radii, uint32_t *keys,
+                                                         int32_t *vals, KeyHist h) {
+    __shared__ unsigned sh[kMaxPasses][kRadix];
+    key_hist_zero(sh);
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = radii[i] > 0 ? __float_as_uint(depths[i]) : 0xffffffffu;
+        keys[i] = k;
+        vals[i] = i;
+        key_hist_add(h, sh, k);
+    }
+    __syncthreads();
+    key_hist_flush(h, sh);
+}
+
+// Blocks of the depth-key pass: about 16 keys per thread, at most 8 per SM.
+static unsigned depth_key_blocks(long long n) {
+    return (unsigned)std::max(1ll, std::min(152ll * 8, (n + 256 * 16 - 1) / (256 * 16)));
 }
 
 // ---------------------------------------------------------------------------
@@ -527,10 +585,12 @@ struct EmitExpandArgs {
     uint32_t *tile_out;
     int32_t *id_out;
     uint32_t *status;
+    KeyHist hist;  // the tile sort's digit counts of the written keys
 };
 
 template <class Grid>
 __global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs<Grid> a) {
+    __shared__ unsigned s_hist[kMaxPasses][kRadix];
     __shared__ int s_off[kEmitBlock];
     __shared__ int4 s_info[kEmitBlock];  // (first tile, tiles per row of the grid, width, id)
     __shared__ float s_rw[kEmitBlock];   // 1 / width
@@ -540,6 +600,7 @@ __global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs<
     const int k = k0 + t;
     const int last = min(a.n, k0 + kEmitBlock) - 1;
     const int base = a.offs[k0];
+    key_hist_zero(s_hist);
     int cnt = 0;
     if (k < a.n) {
         const int g = a.order[k];
@@ -591,9 +652,13 @@ __global__ void __launch_bounds__(kEmitBlock) emit_expand_kernel(EmitExpandArgs<
         if (rx < 0) { --qy; rx += w; }
         if (rx >= w) { ++qy; rx -= w; }
         const int slot = base + s;
-        a.tile_out[slot] = (uint32_t)(info.x + qy * info.y + rx);
+        const uint32_t key = (uint32_t)(info.x + qy * info.y + rx);
+        a.tile_out[slot] = key;
         a.id_out[slot] = info.w;
+        key_hist_add(a.hist, s_hist, key);
     }
+    __syncthreads();
+    key_hist_flush(a.hist, s_hist);
 }
 
 // ---------------------------------------------------------------------------
@@ -776,12 +841,15 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
         if (int rc = check_launch("emit_ref_kernel")) return rc;
     }
     // 1. Gaussians by depth
-    depth_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, depths, radii, L.g.ka, L.g.va);
+    if (int rc = radix_clear(L.g, s)) return rc;
+    depth_keys_kernel<<<depth_key_blocks(n), 256, 0, s>>>(n, depths, radii, L.g.ka, L.g.va,
+                                                          key_hist(L.g, 32));
     if (int rc = check_launch("depth_keys_kernel")) return rc;
     const uint32_t *gkeys;
     const int32_t *order;
     const Count all{nullptr, n, n};
-    if (int rc = radix_sort(p.device_status, spin_limit(p), L.g, all, 32, nullptr, &gkeys, &order, s))
+    if (int rc = radix_sort(p.device_status, spin_limit(p), L.g, all, 32, nullptr, &gkeys, &order, s,
+                            true))
         return rc;
     // 2. emission in depth order
     const int oblocks = (n + kOffPart - 1) / kOffPart;
@@ -811,14 +879,16 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
     e.tile_out = L.s.ka;
     e.id_out = L.s.va;
     e.status = p.device_status;
+    const int tile_bits = std::max(1, bit_length(T - 1));
+    e.hist = key_hist(L.s, tile_bits);
+    if (int rc = radix_clear(L.s, s)) return rc;
     emit_expand_kernel<<<(n + kEmitBlock - 1) / kEmitBlock, kEmitBlock, 0, s>>>(e);
     if (int rc = check_launch("emit_expand_kernel")) return rc;
     // 3. stable sort by tile id
-    const int tile_bits = std::max(1, bit_length(T - 1));
     const uint32_t *tiles_sorted;
     const int32_t *ids_final;
     if (int rc = radix_sort(p.device_status, spin_limit(p), L.s, count, tile_bits, ids_sorted,
-                            &tiles_sorted, &ids_final, s))
+                            &tiles_sorted, &ids_final, s, true))
         return rc;
     if (keys_sorted_out) {
         compose_keys_kernel<<<(unsigned)((count.cap + 255) / 256), 256, 0, s>>>(
@@ -887,12 +957,15 @@ int launch_batch_sort_and_bin(const splat_batch &b, Count count, const float *xy
     const uint32_t spin = spin_limit(b);
     if (count.cap > 0 && e > 0) {
         // 1. entries by depth
-        depth_keys_kernel<<<(e + 255) / 256, 256, 0, s>>>(e, depths, radii, L.g.ka, L.g.va);
+        if (int rc = radix_clear(L.g, s)) return rc;
+        depth_keys_kernel<<<depth_key_blocks(e), 256, 0, s>>>(e, depths, radii, L.g.ka, L.g.va,
+                                                              key_hist(L.g, 32));
         if (int rc = check_launch("depth_keys_kernel")) return rc;
         const uint32_t *gkeys;
         const int32_t *order_d;
         const Count all{nullptr, e, e};
-        if (int rc = radix_sort(b.device_status, spin, L.g, all, 32, nullptr, &gkeys, &order_d, s))
+        if (int rc = radix_sort(b.device_status, spin, L.g, all, 32, nullptr, &gkeys, &order_d, s,
+                                true))
             return rc;
         // 2. emission in depth order, each entry into its view's tiles
         const int oblocks = (e + kOffPart - 1) / kOffPart;
@@ -923,14 +996,16 @@ int launch_batch_sort_and_bin(const splat_batch &b, Count count, const float *xy
         ex.tile_out = L.s.ka;
         ex.id_out = L.s.va;
         ex.status = b.device_status;
+        const int tile_bits = std::max(1, bit_length((unsigned)(T - 1)));
+        ex.hist = key_hist(L.s, tile_bits);
+        if (int rc = radix_clear(L.s, s)) return rc;
         emit_expand_kernel<<<(e + kEmitBlock - 1) / kEmitBlock, kEmitBlock, 0, s>>>(ex);
         if (int rc = check_launch("emit_expand_kernel")) return rc;
         // 3. stable sort by global tile id; 4. bins
-        const int tile_bits = std::max(1, bit_length((unsigned)(T - 1)));
         const uint32_t *tiles_sorted;
         const int32_t *ids_final;
         if (int rc = radix_sort(b.device_status, spin, L.s, count, tile_bits, ids_sorted,
-                                &tiles_sorted, &ids_final, s))
+                                &tiles_sorted, &ids_final, s, true))
             return rc;
         tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(tiles_sorted, count, T, bins);
         if (int rc = check_launch("tile_bins_kernel")) return rc;
