@@ -444,9 +444,9 @@ __global__ void __launch_bounds__(256) depth_keys_kernel(int n, const float *dep
     key_hist_flush(h, sh);
 }
 
-// Blocks of the depth-key pass: about 16 keys per thread, at most 8 per SM.
+// Blocks of the depth-key pass: about 4 keys per thread, at most 8 per SM.
 static unsigned depth_key_blocks(long long n) {
-    return (unsigned)std::max(1ll, std::min(152ll * 8, (n + 256 * 16 - 1) / (256 * 16)));
+    return (unsigned)std::max(1ll, std::min(152ll * 8, (n + 256 * 4 - 1) / (256 * 4)));
 }
 
 // ---------------------------------------------------------------------------
