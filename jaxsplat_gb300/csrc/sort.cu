@@ -239,6 +239,16 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     // warp-striped: warp w owns keys [base, base + 32*items), item k of lane l
     // is key base + 32k + l, so (k, l) order is key order
     const int base = part * kPartKeys + warp * 32 * kSortItems + lane;
+    // the partition's values are read only after the ranking: start bringing
+    // them into L2 now (whole 16-byte chunks, from a 16-byte aligned start:
+    // partitions are 16 KB apart, so only the buffer's own alignment matters)
+    if (t == 0) {
+        const int32_t *src = a.vals_in + (size_t)part * kPartKeys;
+        const uint32_t bytes = (uint32_t)(min(count - part * kPartKeys, kPartKeys) * 4) & ~15u;
+        if (bytes && (reinterpret_cast<uintptr_t>(src) & 15u) == 0)
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes)
+                         : "memory");
+    }
 
     uint32_t key[kSortItems];
     unsigned rank[kSortItems];
