@@ -763,26 +763,50 @@ __global__ void compose_keys_kernel(Count count, const uint32_t *tiles, const in
 }
 
 // ---------------------------------------------------------------------------
-// Tile bin edges: one thread per tile, binary search over the sorted tile ids.
-// Writes every tile, (0, 0) when empty, so no zeroing pass is needed (the
-// reference memsets then marks the boundaries, forward.cu:184-208).
+// Tile bin edges by search over the sorted tile ids.  Writes every tile,
+// (0, 0) when empty, so no zeroing pass is needed (the reference memsets then
+// marks the boundaries, forward.cu:184-208).
 
-__device__ __forceinline__ long long lower_tile(const uint32_t *keys, long long count, uint32_t tile) {
-    long long lo = 0, hi = count;
-    while (lo < hi) {
-        const long long mid = (lo + hi) >> 1;
-        if (keys[mid] < tile) lo = mid + 1; else hi = mid;
+
+// One warp per tile: lanes 0-15 find the first key >= t, lanes 16-31 the
+// first key >= t + 1, each half by a 16-way search (16 probes per step, a
+// ballot picks the interval), so a tile costs ~6 dependent loads instead of
+// the ~2 log2(I) of a binary search.  Invariant: the answer lies in [lo, hi].
+__global__ void __launch_bounds__(256) tile_bins_kernel(const uint32_t *keys, Count cnt,
+                                                        int ntiles, int2 *bins) {
+    const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+    const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (t >= ntiles) return;  // whole warps
+    const uint32_t x = (uint32_t)t + (uint32_t)half;
+    long long lo = 0, hi = cnt.get();
+    for (;;) {
+        const bool active = hi - lo > 16;
+        if (!__any_sync(0xffffffffu, active)) break;
+        const long long step = (hi - lo + 15) >> 4;
+        const long long idx = lo + hl * step;
+        const bool ge = !active || idx >= hi || keys[idx] >= x;
+        const unsigned b = (__ballot_sync(0xffffffffu, ge) >> (half * 16)) & 0xffffu;
+        if (active) {
+            if (b == 0) {
+                lo += 15 * step + 1;  // every probe < x
+            } else {
+                const int f = __ffs(b) - 1;
+                if (f == 0) {
+                    hi = lo;  // keys[lo] >= x
+                } else {
+                    const long long p = lo + f * step;
+                    lo += (f - 1) * step + 1;
+                    hi = min(hi, p);
+                }
+            }
+        }
     }
-    return lo;
-}
-
-__global__ void tile_bins_kernel(const uint32_t *keys, Count cnt, int ntiles, int2 *bins) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntiles) return;
-    const long long count = cnt.get();
-    const long long lo = lower_tile(keys, count, (uint32_t)t);
-    const long long hi = lower_tile(keys, count, (uint32_t)t + 1);
-    bins[t] = lo < hi ? make_int2((int)lo, (int)hi) : make_int2(0, 0);
+    const long long idx = lo + hl;
+    const bool ge = idx >= hi || keys[idx] >= x;
+    const unsigned b = (__ballot_sync(0xffffffffu, ge) >> (half * 16)) & 0xffffu;
+    const long long first = b ? lo + (__ffs(b) - 1) : hi;
+    const long long next = __shfl_sync(0xffffffffu, first, 16);
+    if (lane == 0) bins[t] = first < next ? make_int2((int)first, (int)next) : make_int2(0, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -907,7 +931,8 @@ int launch_sort_and_bin(const splat_params &p, Count count, const float *xys,
         if (int rc = check_launch("compose_keys_kernel")) return rc;
     }
     // 4. bins
-    tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(tiles_sorted, count, (int)T, bins);
+    tile_bins_kernel<<<(unsigned)(((long long)T * 32 + 255) / 256), 256, 0, s>>>(tiles_sorted, count,
+                                                                           (int)T, bins);
     return check_launch("tile_bins_kernel");
 }
 
@@ -1017,7 +1042,8 @@ int launch_batch_sort_and_bin(const splat_batch &b, Count count, const float *xy
         if (int rc = radix_sort(b.device_status, spin, L.s, count, tile_bits, ids_sorted,
                                 &tiles_sorted, &ids_final, s, true))
             return rc;
-        tile_bins_kernel<<<(T + 255) / 256, 256, 0, s>>>(tiles_sorted, count, T, bins);
+        tile_bins_kernel<<<(unsigned)(((long long)T * 32 + 255) / 256), 256, 0, s>>>(
+            tiles_sorted, count, (int)T, bins);
         if (int rc = check_launch("tile_bins_kernel")) return rc;
     } else if (cudaMemsetAsync(bins, 0, sizeof(int2) * (size_t)T, s) != cudaSuccess) {
         return check_launch("tile_bins memset");
