@@ -16,7 +16,9 @@
  *
  *  2. splat_*: typed entry points with plain pointers, sizes, an explicit
  *     stream, caller-provided workspace (size from the *_workspace_size
- *     query) and an int status.  No allocation, no host synchronisation
+ *     query, 256-byte aligned: it holds words updated by 64-bit atomics;
+ *     a misaligned one is refused with SPLAT_ERR_INVALID_ARG) and an int
+ *     status.  No allocation, no host synchronisation
  *     (except splat_read_counts, which exists to read the count).
  *
  * All arrays are row-major, C-contiguous, fp32 unless marked, with the

@@ -86,6 +86,15 @@ static int check_count(long long count) {
         if (!(ptr)) return fail(SPLAT_ERR_INVALID_ARG, "%s is NULL", #ptr);               \
     } while (0)
 
+// Workspaces hold 64-bit words updated by atomics and vector-loaded arrays:
+// 256-byte aligned, as every device allocator returns them.
+#define NEED_WS(ptr)                                                                       \
+    do {                                                                                   \
+        NEED(ptr);                                                                         \
+        if (reinterpret_cast<uintptr_t>(ptr) % 256)                                        \
+            return fail(SPLAT_ERR_INVALID_ARG, "%s must be 256-byte aligned", #ptr);       \
+    } while (0)
+
 static size_t project_ws_bytes(const splat_params &p) {
     // one look-back word per partition (4096 Gaussians; sized per 256)
     const size_t parts = (p.num_points + 255) / 256;
@@ -230,7 +239,7 @@ static int project_fwd_entry(const splat_params *p, const float *means3d, const 
     }
     NEED(means3d); NEED(scales); NEED(quats); NEED(viewmat); NEED(cov3d); NEED(xys);
     NEED(depths); NEED(radii); NEED(conics); NEED(compensation); NEED(num_tiles_hit);
-    NEED(cum_tiles_hit); NEED(workspace);
+    NEED(cum_tiles_hit); NEED_WS(workspace);
     if (workspace_bytes < project_ws_bytes(*p))
         return fail(SPLAT_ERR_WORKSPACE, "project workspace too small: need %zu, got %zu",
                     project_ws_bytes(*p), workspace_bytes);
@@ -319,7 +328,7 @@ int splat_sort_and_bin(const splat_params *p, int64_t num_intersects, const int6
     if (int rc = check_count(num_intersects)) return rc;
     NEED(tile_bins);
     if (num_intersects > 0) {
-        NEED(xys); NEED(depths); NEED(radii); NEED(gaussian_ids_sorted); NEED(workspace);
+        NEED(xys); NEED(depths); NEED(radii); NEED(gaussian_ids_sorted); NEED_WS(workspace);
         if (isect_ids) NEED(cum_tiles_hit);
     }
     const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};

@@ -336,6 +336,11 @@ int splat_batch_sort_and_bin(const splat_batch *b, int64_t capacity, const int64
     if (int rc = check_batch(b)) return rc;
     if (int rc = check_capacity(capacity)) return rc;
     NEED(count_dev); NEED(xys); NEED(depths); NEED(radii); NEED(tile_bins); NEED(tile_order);
+    NEED(workspace);
+    // 64-bit look-back words updated by atomics: 256-byte aligned, as every
+    // device allocator returns it
+    if (reinterpret_cast<uintptr_t>(workspace) % 256)
+        return fail(SPLAT_ERR_INVALID_ARG, "workspace must be 256-byte aligned");
     if (capacity > 0) NEED(gaussian_ids_sorted);
     const Count c{reinterpret_cast<const long long *>(count_dev), 0, capacity};
     return launch_batch_sort_and_bin(*b, c, xys, depths, radii, gaussian_ids_sorted,

@@ -91,3 +91,18 @@ def test_strings(lib):
     assert lib.splat_status_string(4) == b"intersection count out of range"
     assert b"lookback-timeout" in lib.splat_device_status_string(1)
     assert lib.splat_version() >= 1
+
+
+def test_misaligned_workspace_rejected_without_gpu(lib):
+    """Workspaces must be 256-byte aligned (they hold words updated by 64-bit
+    atomics); a misaligned one is refused before any CUDA call.  The other
+    pointers are placeholders that are never dereferenced."""
+    from jaxsplat_gb300 import _lib
+
+    p = _lib.make_params(10, (32, 32), (32.0, 32.0), (16.0, 16.0), 1.0, 0.01, 16)
+    fake = [C.c_void_p(0x10000 + 256 * i) for i in range(13)]
+    rc = lib.splat_project_fwd(C.byref(p), *fake, C.c_void_p(0x20008), 1 << 20, None)
+    assert rc == 1 and b"256-byte aligned" in lib.splat_last_error()
+    rc = lib.splat_sort_and_bin(C.byref(p), 100, None, *fake[:4], fake[4], fake[5], None, None,
+                                None, C.c_void_p(0x20010), 1 << 20, None)
+    assert rc == 1 and b"256-byte aligned" in lib.splat_last_error()
