@@ -18,7 +18,8 @@
  *     stream, caller-provided workspace (size from the *_workspace_size
  *     query, 256-byte aligned: it holds words updated by 64-bit atomics;
  *     a misaligned one is refused with SPLAT_ERR_INVALID_ARG) and an int
- *     status.  No allocation, no host synchronisation
+ *     status.  tile_bins must be 8-byte aligned (read and written as int2)
+ *     and packed 16-byte aligned (float4 records).  No allocation, no host synchronisation
  *     (except splat_read_counts, which exists to read the count).
  *
  * All arrays are row-major, C-contiguous, fp32 unless marked, with the

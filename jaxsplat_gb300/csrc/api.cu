@@ -86,6 +86,14 @@ static int check_count(long long count) {
         if (!(ptr)) return fail(SPLAT_ERR_INVALID_ARG, "%s is NULL", #ptr);               \
     } while (0)
 
+// tile_bins is read and written as int2
+#define NEED_BINS(ptr)                                                                     \
+    do {                                                                                   \
+        NEED(ptr);                                                                         \
+        if (reinterpret_cast<uintptr_t>(ptr) % 8)                                          \
+            return fail(SPLAT_ERR_INVALID_ARG, "%s must be 8-byte aligned", #ptr);         \
+    } while (0)
+
 // Workspaces hold 64-bit words updated by atomics and vector-loaded arrays:
 // 256-byte aligned, as every device allocator returns them.
 #define NEED_WS(ptr)                                                                       \
@@ -326,7 +334,7 @@ int splat_sort_and_bin(const splat_params *p, int64_t num_intersects, const int6
                        splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     if (int rc = check_count(num_intersects)) return rc;
-    NEED(tile_bins);
+    NEED_BINS(tile_bins);
     if (num_intersects > 0) {
         NEED(xys); NEED(depths); NEED(radii); NEED(gaussian_ids_sorted); NEED_WS(workspace);
         if (isect_ids) NEED(cum_tiles_hit);
@@ -358,7 +366,7 @@ int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int
     if (int rc = check_count(num_intersects)) return rc;
     NEED(background); NEED(final_Ts); NEED(final_idx); NEED(out_img);
     if (num_intersects > 0) {
-        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed);
+        NEED(gaussian_ids_sorted); NEED_BINS(tile_bins); NEED(packed);
         if (reinterpret_cast<uintptr_t>(packed) % 16)
             return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
     }
@@ -379,7 +387,7 @@ int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersects, const 
     NEED(background); NEED(target); NEED(final_Ts); NEED(final_idx); NEED(out_img);
     NEED(v_img); NEED(loss_out);
     if (num_intersects > 0) {
-        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed);
+        NEED(gaussian_ids_sorted); NEED_BINS(tile_bins); NEED(packed);
         if (reinterpret_cast<uintptr_t>(packed) % 16)
             return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
     }
@@ -398,7 +406,7 @@ int splat_count_pairs(const splat_params *p, int64_t num_intersects, const int64
     if (int rc = check_count(num_intersects)) return rc;
     NEED(counts);
     if (num_intersects > 0) {
-        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed); NEED(final_idx);
+        NEED(gaussian_ids_sorted); NEED_BINS(tile_bins); NEED(packed); NEED(final_idx);
         if (reinterpret_cast<uintptr_t>(packed) % 16)
             return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");
     }
@@ -420,7 +428,7 @@ int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects, const int
         NEED(v_colors); NEED(v_opacity); NEED(v_xy); NEED(v_conic);
     }
     if (num_intersects > 0) {
-        NEED(gaussian_ids_sorted); NEED(tile_bins); NEED(packed); NEED(background);
+        NEED(gaussian_ids_sorted); NEED_BINS(tile_bins); NEED(packed); NEED(background);
         NEED(final_Ts); NEED(final_idx); NEED(v_img); NEED(v_img_alpha);
         if (reinterpret_cast<uintptr_t>(packed) % 16)
             return fail(SPLAT_ERR_INVALID_ARG, "packed must be 16-byte aligned");

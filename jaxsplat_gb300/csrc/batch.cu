@@ -225,6 +225,14 @@ using namespace splat;
         if (!(ptr)) return fail(SPLAT_ERR_INVALID_ARG, "%s must not be NULL", #ptr);   \
     } while (0)
 
+// tile_bins is read and written as int2
+#define NEED_BINS(ptr)                                                                     \
+    do {                                                                                   \
+        NEED(ptr);                                                                         \
+        if (reinterpret_cast<uintptr_t>(ptr) % 8)                                          \
+            return fail(SPLAT_ERR_INVALID_ARG, "%s must be 8-byte aligned", #ptr);         \
+    } while (0)
+
 extern "C" {
 
 int splat_batch_layout(splat_batch *b, splat_view *views, const uint32_t *scene_points) {
@@ -335,7 +343,7 @@ int splat_batch_sort_and_bin(const splat_batch *b, int64_t capacity, const int64
                              splat_stream_t stream) {
     if (int rc = check_batch(b)) return rc;
     if (int rc = check_capacity(capacity)) return rc;
-    NEED(count_dev); NEED(xys); NEED(depths); NEED(radii); NEED(tile_bins); NEED(tile_order);
+    NEED(count_dev); NEED(xys); NEED(depths); NEED(radii); NEED_BINS(tile_bins); NEED(tile_order);
     NEED(workspace);
     // 64-bit look-back words updated by atomics: 256-byte aligned, as every
     // device allocator returns it
@@ -365,7 +373,7 @@ int splat_batch_rasterize_fwd(const splat_batch *b, int64_t capacity, const int6
                               int32_t *work_counter, splat_stream_t stream) {
     if (int rc = check_batch(b)) return rc;
     if (int rc = check_capacity(capacity)) return rc;
-    NEED(count_dev); NEED(tile_bins); NEED(tile_order); NEED(packed); NEED(final_Ts);
+    NEED(count_dev); NEED_BINS(tile_bins); NEED(tile_order); NEED(packed); NEED(final_Ts);
     NEED(final_idx); NEED(out_img); NEED(work_counter);
     if (capacity > 0) NEED(gaussian_ids_sorted);
     if (chunk < 1 || chunk > 64) return fail(SPLAT_ERR_INVALID_ARG, "chunk must be in [1, 64]");
@@ -384,7 +392,7 @@ int splat_batch_rasterize_fwd_l2(const splat_batch *b, int64_t capacity, const i
                                  int32_t *work_counter, splat_stream_t stream) {
     if (int rc = check_batch(b)) return rc;
     if (int rc = check_capacity(capacity)) return rc;
-    NEED(count_dev); NEED(tile_bins); NEED(tile_order); NEED(packed); NEED(target);
+    NEED(count_dev); NEED_BINS(tile_bins); NEED(tile_order); NEED(packed); NEED(target);
     NEED(final_Ts); NEED(final_idx); NEED(out_img); NEED(v_img); NEED(loss_out);
     NEED(work_counter);
     if (capacity > 0) NEED(gaussian_ids_sorted);
@@ -405,7 +413,7 @@ int splat_batch_rasterize_bwd(const splat_batch *b, int64_t capacity, const int6
                               int32_t *work_counter, splat_stream_t stream) {
     if (int rc = check_batch(b)) return rc;
     if (int rc = check_capacity(capacity)) return rc;
-    NEED(count_dev); NEED(tile_bins); NEED(tile_order); NEED(packed); NEED(final_Ts);
+    NEED(count_dev); NEED_BINS(tile_bins); NEED(tile_order); NEED(packed); NEED(final_Ts);
     NEED(final_idx); NEED(v_img); NEED(v_img_alpha); NEED(v_colors); NEED(v_opacity);
     NEED(v_xy); NEED(v_conic); NEED(work_counter);
     if (capacity > 0) NEED(gaussian_ids_sorted);

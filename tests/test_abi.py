@@ -106,3 +106,15 @@ def test_misaligned_workspace_rejected_without_gpu(lib):
     rc = lib.splat_sort_and_bin(C.byref(p), 100, None, *fake[:4], fake[4], fake[5], None, None,
                                 None, C.c_void_p(0x20010), 1 << 20, None)
     assert rc == 1 and b"256-byte aligned" in lib.splat_last_error()
+
+
+def test_misaligned_tile_bins_rejected_without_gpu(lib):
+    """tile_bins is accessed as int2: a 4-byte offset is refused before any
+    CUDA call."""
+    from jaxsplat_gb300 import _lib
+
+    p = _lib.make_params(10, (32, 32), (32.0, 32.0), (16.0, 16.0), 1.0, 0.01, 16)
+    fake = [C.c_void_p(0x10000 + 256 * i) for i in range(8)]
+    rc = lib.splat_rasterize_fwd(C.byref(p), 100, None, fake[0], C.c_void_p(0x30004), fake[1],
+                                 fake[2], fake[3], fake[4], fake[5], None)
+    assert rc == 1 and b"8-byte aligned" in lib.splat_last_error()
