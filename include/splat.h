@@ -107,7 +107,10 @@ SPLAT_API int splat_project_fwd(const splat_params *p, const float *means3d, con
  * (splat_pack_splats' output, bit-identical) from each Gaussian's projection
  * and its colour and opacity, so that no separate packing pass runs.  No
  * reference counterpart (the reference has no packing pass).  Same workspace.
- *   colors (N,3) opacities (N,1) -> packed (N,12), 16-byte aligned */
+ *   colors (N,3) opacities (N,1) -> packed (N,12), 16-byte aligned
+ * cum_tiles_hit may be NULL here: the projection then only adds up the
+ * intersection count into total_out (one atomic per block) instead of
+ * scanning the tile counts. */
 SPLAT_API int splat_project_fwd_packed(const splat_params *p, const float *means3d,
                                        const float *scales, const float *quats,
                                        const float *viewmat, const float *colors,

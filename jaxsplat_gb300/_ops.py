@@ -63,10 +63,11 @@ def _workspace(nbytes: int, device) -> torch.Tensor:
 # project
 
 def project_fwd(means3d, scales, quats, viewmat, *, img_shape, f, c, glob_scale, clip_thresh,
-                block_width, colors=None, opacities=None):
+                block_width, colors=None, opacities=None, with_cum=True):
     """lib/ops.cu:12-61 -> dict(cov3d, xys, depths, radii, conics, compensation,
     num_tiles_hit, cum_tiles_hit, total); with colors and opacities also the
-    packed rasterizer records ("packed", splat_project_fwd_packed)."""
+    packed rasterizer records ("packed", splat_project_fwd_packed), and then
+    with_cum=False skips cum_tiles_hit (only the total is formed)."""
     lib = _lib.load()
     n = means3d.shape[0]
     dev = means3d.device
@@ -100,9 +101,11 @@ def project_fwd(means3d, scales, quats, viewmat, *, img_shape, f, c, glob_scale,
         C.byref(p), _ptr(means3d), _ptr(scales), _ptr(quats), _ptr(viewmat), _ptr(colors),
         _ptr(opacities), _ptr(out["cov3d"]), _ptr(out["xys"]), _ptr(out["depths"]),
         _ptr(out["radii"]), _ptr(out["conics"]), _ptr(out["compensation"]),
-        _ptr(out["num_tiles_hit"]), _ptr(out["cum_tiles_hit"]), _ptr(out["total"]),
-        _ptr(out["packed"]), _ptr(ws), ws.numel(), _stream())
+        _ptr(out["num_tiles_hit"]), _ptr(out["cum_tiles_hit"]) if with_cum else None,
+        _ptr(out["total"]), _ptr(out["packed"]), _ptr(ws), ws.numel(), _stream())
     _lib.check(rc, "project_fwd_packed")
+    if not with_cum:
+        del out["cum_tiles_hit"]
     return out
 
 

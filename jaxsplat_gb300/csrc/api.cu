@@ -247,7 +247,8 @@ static int project_fwd_entry(const splat_params *p, const float *means3d, const 
     }
     NEED(means3d); NEED(scales); NEED(quats); NEED(viewmat); NEED(cov3d); NEED(xys);
     NEED(depths); NEED(radii); NEED(conics); NEED(compensation); NEED(num_tiles_hit);
-    NEED(cum_tiles_hit); NEED_WS(workspace);
+    if (!packed) NEED(cum_tiles_hit);  // optional only with the packed records
+    NEED_WS(workspace);
     if (workspace_bytes < project_ws_bytes(*p))
         return fail(SPLAT_ERR_WORKSPACE, "project workspace too small: need %zu, got %zu",
                     project_ws_bytes(*p), workspace_bytes);

@@ -117,6 +117,14 @@ __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a
         incl[r] = run + block_scan(hits, s_warp, &round_total);
         run += round_total;
     }
+    if (a.cum == nullptr) {  // only the total is wanted: one atomic per block
+        if (threadIdx.x == 0 && run) {
+            const unsigned long long old =
+                atomicAdd(reinterpret_cast<unsigned long long *>(a.total), run);
+            if (old + run > 0x7fffffffull) raise_status(a.status, DEV_SCAN_OVERFLOW);
+        }
+        return;
+    }
 
     // partition prefix by decoupled look-back (64-bit carries)
     if (threadIdx.x < 32) {
@@ -205,6 +213,9 @@ int launch_project_fwd(const splat_params &p, const float *means3d, const float 
     const int nparts = (n + rounds * kProjThreads - 1) / (rounds * kProjThreads);
     if (cudaMemsetAsync(words, 0, sizeof(unsigned long long) * (size_t)(nparts + 1), s) != cudaSuccess)
         return check_launch("project_fwd workspace memset");
+    // without cum_tiles_hit the blocks add their counts to the total
+    if (!cum && cudaMemsetAsync(total, 0, sizeof(int64_t), s) != cudaSuccess)
+        return check_launch("project_fwd total memset");
     ProjFwdArgs a;
     a.n = n;
     a.means3d = means3d; a.scales = scales; a.quats = quats; a.viewmat = viewmat;

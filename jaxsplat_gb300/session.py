@@ -155,11 +155,12 @@ class RenderSession(StreamingSteps):
 
     def _project(self, pack=False):
         P, pr = self._p, C.byref(self.params)
-        if pack:  # the packed records too (no separate packing pass)
+        if pack:  # the packed records too (no separate packing pass), and only the
+            # intersection count: the step never reads cum_tiles_hit
             self._check(self.lib.splat_project_fwd_packed(
                 pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat),
                 P(self.colors), P(self.opacities), P(self.cov3d), P(self.xys), P(self.depths),
-                P(self.radii), P(self.conics), P(self.comp), P(self.ntiles), P(self.cum),
+                P(self.radii), P(self.conics), P(self.comp), P(self.ntiles), None,
                 P(self.total), P(self.packed), P(self.proj_ws), self.proj_ws.numel(),
                 self._stream()), "project_fwd_packed")
             return

@@ -38,6 +38,12 @@ def test_fused_projection_and_forward_loss(bw):
     for k in a:
         assert torch.equal(a[k], b[k]), k
     assert torch.equal(packed.view(torch.int32), b["packed"].view(torch.int32))
+    # without cum_tiles_hit: the same outputs and the same total
+    c = _ops.project_fwd(t["means3d"], t["scales"], t["quats"], t["viewmat"], **proj_kw,
+                         colors=t["colors"], opacities=t["opacities"], with_cum=False)
+    assert "cum_tiles_hit" not in c
+    for k in c:
+        assert torch.equal(b[k], c[k]), k
 
     n = sc.spec.num_points
     count = _ops.read_counts(n, a["cum_tiles_hit"], a["total"], device=t["means3d"].device)
