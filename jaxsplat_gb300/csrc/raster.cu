@@ -431,7 +431,7 @@ enum { G_R, G_G, G_B, G_CA, G_CB, G_CC, G_X, G_Y, G_OP, G_AX, G_AY, G_FIELDS };
 
 // With at most this many contributing lanes a warp adds per lane into shared
 // memory instead of reducing across the warp first.
-constexpr int kFewLanes = 8;
+constexpr int kFewLanes = 16;
 
 struct RasterBwdArgs {
     unsigned tiles_x, width, height, bw;
