@@ -118,3 +118,27 @@ def test_misaligned_tile_bins_rejected_without_gpu(lib):
     rc = lib.splat_rasterize_fwd(C.byref(p), 100, None, fake[0], C.c_void_p(0x30004), fake[1],
                                  fake[2], fake[3], fake[4], fake[5], None)
     assert rc == 1 and b"8-byte aligned" in lib.splat_last_error()
+
+
+def test_xla_module_mirrors_the_reference_native_module(lib):
+    """jaxsplat_gb300.xla: registrations() gives the four custom-call targets
+    as PyCapsules named xla._CUSTOM_CALL_TARGET pointing at the splat_xla_*
+    functions; make_descriptor(**kwargs) takes the reference lowering's
+    keyword arguments and returns the 80-byte descriptor."""
+    from jaxsplat_gb300 import xla
+
+    regs = xla.registrations()
+    assert set(regs) == {"project_fwd", "project_bwd", "rasterize_fwd", "rasterize_bwd"}
+    get_name = C.pythonapi.PyCapsule_GetName
+    get_name.restype, get_name.argtypes = C.c_char_p, [C.py_object]
+    get_ptr = C.pythonapi.PyCapsule_GetPointer
+    get_ptr.restype, get_ptr.argtypes = C.c_void_p, [C.py_object, C.c_char_p]
+    for name, cap in regs.items():
+        assert get_name(cap) == b"xla._CUSTOM_CALL_TARGET"
+        want = C.cast(getattr(lib, "splat_xla_" + name), C.c_void_p).value
+        assert get_ptr(cap, b"xla._CUSTOM_CALL_TARGET") == want
+    d = xla.make_descriptor(num_points=100_000, img_shape=(1080, 1920), f=(1200.0, 1100.0),
+                            c=(960.0, 540.0), glob_scale=1.0, clip_thresh=0.01, block_width=16)
+    want = struct.pack("<I3I4f", 100_000, 1920, 1080, 1, 1200.0, 1100.0, 960.0, 540.0)
+    want += struct.pack("<ffII I3I3I", 1.0, 0.01, 16, 391, 256, 120, 68, 1, 16, 16, 1)
+    assert d == want + b"\0" * (80 - len(want))
