@@ -1,17 +1,26 @@
 """Benchmark: forward+backward of the render path, 1M Gaussians at 1920x1080.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--scene hd|uhd|small] [--no-cpu-baseline]
+                    [--scene hd|uhd|small|batch|fit|warmstart] [--no-cpu-baseline]
 
-One step = project -> count read -> sort/bin -> rasterize forward -> L2 loss
-against a target image -> rasterize backward -> project backward, on seeded
-synthetic inputs with the benchmark scene's shapes and distributions.
+One step = project -> sort/bin -> rasterize forward with the L2 loss against
+a target image -> rasterize backward -> project backward (one CUDA graph, the
+intersection count kept on the device), on seeded synthetic inputs with the
+benchmark scene's shapes and distributions.
 
 * ``value``: ms per step with inputs resident in HBM, CUDA events on the
   launching stream, L2 flushed (a 256 MiB write) before every timed step and
   excluded from the timing.
 * ``e2e``: the same step with the inputs copied from pinned host memory and
-  the loss and the five gradient arrays copied back inside the timed region.
+  the loss and the five gradient arrays copied back inside the timed region,
+  one step at a time (``RenderSession.step_io``), with the host link's
+  measured bandwidth (``link_gbs``).
+* ``e2e_streamed``: consecutive steps through ``stream_step`` (every step
+  still uploads its inputs and downloads its results; double-buffered, so
+  the copies of neighbouring steps overlap the computation).
+* ``roofline``: the dominant kernel's algorithmic bytes over its time against
+  the measured HBM bandwidth, with its ncu DRAM traffic; ``pairs`` and
+  ``stage_roofline``: work counts and each stage's HBM / FP32 / ex2 floor.
 * ``--impl reference``: the reference's own CUDA kernels (built from its
   sources into oracle/_ref) driven with its stock host orchestration
   (oracle/ref_harness.cu) on the same GPU, same workload; when those are not
