@@ -64,3 +64,20 @@ def test_training_lowers_the_loss():
     hist = ws.train(imgs, grids, epochs=30, batch=4, lr=3e-3)
     torch.cuda.synchronize()
     assert hist[-1] < 0.5 * hist[0], hist
+
+
+def test_learned_warm_start_beats_plain_fit():
+    """The learned part's gain over the plain method, small: a network trained
+    on 96 fits of the plain loop proposes initial Gaussians for held-out
+    targets, which then reach 30 dB PSNR in clearly fewer Adam steps than from
+    random init (at full size, 1000 training fits: 35-55 vs 135-170 steps)."""
+    from jaxsplat_gb300.warmstart import run_experiment
+
+    r = run_experiment(n_train=96, fit_steps=150, epochs=20,
+                       eval_seeds=(1_000_000, 1_000_001), check_every=5)
+    assert r["loss_last"] < r["loss_first"]
+    for row in r["eval"]:
+        assert row["plain_reached"] and row["learned_reached"], row
+    learned = sum(row["learned_steps"] for row in r["eval"])
+    plain = sum(row["plain_steps"] for row in r["eval"])
+    assert learned < 0.75 * plain, r["eval"]
