@@ -142,3 +142,11 @@ def test_xla_module_mirrors_the_reference_native_module(lib):
     want = struct.pack("<I3I4f", 100_000, 1920, 1080, 1, 1200.0, 1100.0, 960.0, 540.0)
     want += struct.pack("<ffII I3I3I", 1.0, 0.01, 16, 391, 256, 120, 68, 1, 16, 16, 1)
     assert d == want + b"\0" * (80 - len(want))
+
+
+def test_xla_make_descriptor_rejects_bad_block_width(lib):
+    from jaxsplat_gb300 import _lib, xla
+
+    with pytest.raises(_lib.SplatError):
+        xla.make_descriptor(num_points=10, img_shape=(32, 32), f=(32.0, 32.0), c=(16.0, 16.0),
+                            glob_scale=1.0, clip_thresh=0.01, block_width=0)
