@@ -40,22 +40,81 @@ def test_exports_every_declared_symbol(lib):
     assert sorted(_lib.EXPORTED) == names
 
 
-def test_params_layout_matches_header(tmp_path):
-    from jaxsplat_gb300._lib import SplatParams
+_C_SCALARS = {"int": (4, "i"), "int32_t": (4, "i"), "uint32_t": (4, "u"), "int64_t": (8, "i"),
+              "uint64_t": (8, "u"), "size_t": (8, "u"), "float": (4, "f"), "double": (8, "f")}
 
+
+def _c_kind(decl: str):
+    """'ptr' for pointers and the stream handle, else (bytes, i/u/f)."""
+    decl = decl.strip()
+    if "*" in decl or decl.split()[0] == "splat_stream_t":
+        return "ptr"
+    words = [w for w in decl.split() if w != "const"]
+    return _C_SCALARS[words[0]]
+
+
+def _ctypes_kind(t):
+    if t in (C.c_void_p, C.c_char_p) or issubclass(t, C._Pointer):
+        return "ptr"
+    if t in (C.c_float, C.c_double):
+        return (C.sizeof(t), "f")
+    return (C.sizeof(t), "i" if t(-1).value < 0 else "u")
+
+
+def declared_prototypes():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    protos = {}
+    for ret, name, params in re.findall(r"SPLAT_API\s+([\w\s\*]+?)\s*\b(splat_\w+)\s*\(([^)]*)\)\s*;",
+                                        text):
+        ps = [p for p in (q.strip() for q in params.split(",")) if p and p != "void"]
+        protos[name] = (ret.strip(), ps)
+    return protos
+
+
+def test_ctypes_signatures_match_header():
+    """Every binding in _lib has the header's parameter count, and each
+    parameter (and the result) the same class: pointer, or a scalar of the
+    same width and signedness."""
+    from jaxsplat_gb300 import _lib
+
+    protos = declared_prototypes()
+    assert sorted(protos) == declared_functions()
+    for name, res, args in _lib._SIGS:
+        ret, params = protos[name]
+        assert len(args) == len(params), (name, len(args), len(params))
+        for k, (t, p) in enumerate(zip(args, params)):
+            assert _ctypes_kind(t) == _c_kind(p + " x"), (name, k, p)
+        if ret == "void":
+            assert res is None, name
+        else:
+            assert _ctypes_kind(res) == _c_kind(ret + " x"), (name, ret)
+
+
+@pytest.mark.parametrize("c_name,py_name", [("splat_params", "SplatParams"),
+                                             ("splat_view", "SplatView"),
+                                             ("splat_batch", "SplatBatch")])
+def test_struct_layout_matches_header(tmp_path, c_name, py_name):
+    """Size, and offset and size of every field, of the ctypes mirror against
+    the C compiler's layout of the header's struct."""
+    from jaxsplat_gb300 import _lib
+
+    mirror = getattr(_lib, py_name)
+    fields = [f[0] for f in mirror._fields_]
+    lines = [f'printf("%zu\\n", sizeof({c_name}));']
+    for f in fields:
+        lines.append(f'printf("%zu %zu\\n", offsetof({c_name}, {f}), '
+                     f"sizeof((({c_name} *)0)->{f}));")
     src = tmp_path / "layout.c"
-    src.write_text(
-        '#include <stdio.h>\n#include <stddef.h>\n#include "splat.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu\\n\", sizeof(splat_params),"
-        " offsetof(splat_params, block_width), offsetof(splat_params, device_status),"
-        " offsetof(splat_params, spin_limit)); return 0;}\n")
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "splat.h"\n'
+                   "int main(void){" + "".join(lines) + "return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
-    size, bw, ds, sl = map(int, subprocess.check_output([str(exe)]).split())
-    assert C.sizeof(SplatParams) == size
-    assert SplatParams.block_width.offset == bw
-    assert SplatParams.device_status.offset == ds
-    assert SplatParams.spin_limit.offset == sl
+    out = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    assert C.sizeof(mirror) == out[0], c_name
+    for k, f in enumerate(fields):
+        desc = getattr(mirror, f)
+        assert (desc.offset, desc.size) == (out[1 + 2 * k], out[2 + 2 * k]), (c_name, f)
 
 
 def test_descriptor_matches_reference_layout(lib):
