@@ -72,9 +72,9 @@ def _meets(x, y, hx, hy, x0, x1, y0, y1):
     return ~((x + hx < x0) | (x - hx > x1) | (y + hy < y0) | (y - hy > y1))
 
 
-COUNT_KEYS = ("entries", "tile_contributing", "fwd_walk", "fwd_work", "bwd_walk", "bwd_work",
-              "bwd_valid_pixels", "bwd_atomics", "final_idx_mismatch", "box_culled_contributing",
-              "identity_mismatch")
+COUNT_KEYS = ("entries", "tile_contributing", "fwd_walk", "fwd_work", "fwd_active_lanes",
+              "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics", "final_idx_mismatch",
+              "box_culled_contributing", "identity_mismatch")
 
 
 def _replay_tile(tot, lanes_hist, lo, hi, ox, oy, h, w, ids, xys, con, opac, ex_all, ey_all,
@@ -130,6 +130,8 @@ def _replay_tile(tot, lanes_hist, lo, hi, ox, oy, h, w, ids, xys, con, opac, ex_
         still = rows[:, None] <= lane_done[None, :]
         tot["fwd_walk"] += int(walk.sum())
         tot["fwd_work"] += int((walk & (passes[:, sel] & still).any(axis=1)).sum())
+        # lanes not yet saturated (inside the image) in each walked iteration
+        tot["fwd_active_lanes"] += int((still & inside[sel][None, :])[walk].sum())
 
     for W in range(4):
         x0, y0 = (W & 1) * 8, (W >> 1) * 8
@@ -209,7 +211,8 @@ def _main():
     st = walk_stats(make_scene("hd", seed=0), tiles=tiles)
     hist = st.pop("lanes_hist")
     print({k: v for k, v in st.items()})
-    print(f"forward iterations that do work:  {st['fwd_work'] / st['fwd_walk']:.3f}")
+    print(f"forward iterations that do work:  {st['fwd_work'] / st['fwd_walk']:.3f}; lanes not "
+          f"yet saturated per walked iteration: {st['fwd_active_lanes'] / st['fwd_walk']:.1f} of 32")
     print(f"backward iterations that do work: {st['bwd_work'] / st['bwd_walk']:.3f}")
     print(f"entries contributing somewhere in their tile: "
           f"{st['tile_contributing'] / st['entries']:.3f}")
