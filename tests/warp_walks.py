@@ -72,9 +72,9 @@ def _meets(x, y, hx, hy, x0, x1, y0, y1):
     return ~((x + hx < x0) | (x - hx > x1) | (y + hy < y0) | (y - hy > y1))
 
 
-COUNT_KEYS = ("entries", "tile_contributing", "fwd_walk", "fwd_work", "fwd_active_lanes",
-              "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics", "final_idx_mismatch",
-              "box_culled_contributing", "identity_mismatch")
+COUNT_KEYS = ("entries", "tile_contributing", "past_saturation", "fwd_walk", "fwd_work",
+              "fwd_active_lanes", "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics",
+              "final_idx_mismatch", "box_culled_contributing", "identity_mismatch")
 
 
 def _replay_tile(tot, lanes_hist, lo, hi, ox, oy, h, w, ids, xys, con, opac, ex_all, ey_all,
@@ -114,6 +114,8 @@ def _replay_tile(tot, lanes_hist, lo, hi, ox, oy, h, w, ids, xys, con, opac, ex_
             break
     tot["entries"] += L
     tot["tile_contributing"] += int(blended.any(axis=1).sum())
+    # entries after the last one any pixel of the tile evaluates
+    tot["past_saturation"] += max(0, L - 1 - int(done_at[inside].max(initial=-1)))
     last = np.where(blended.any(axis=0), L - 1 - np.argmax(blended[::-1], axis=0), -1)
     replay_fidx = np.where(last >= 0, lo + last, 0)
     fid = np.where(inside, fidx_img[np.minimum(pyi, h - 1), np.minimum(pxi, w - 1)], 0)
@@ -215,7 +217,8 @@ def _main():
           f"yet saturated per walked iteration: {st['fwd_active_lanes'] / st['fwd_walk']:.1f} of 32")
     print(f"backward iterations that do work: {st['bwd_work'] / st['bwd_walk']:.3f}")
     print(f"entries contributing somewhere in their tile: "
-          f"{st['tile_contributing'] / st['entries']:.3f}")
+          f"{st['tile_contributing'] / st['entries']:.3f}; past the saturation of every pixel "
+          f"of their tile: {st['past_saturation'] / st['entries']:.3f}")
     print(f"backward, per iteration that does work: "
           f"{st['bwd_valid_pixels'] / st['bwd_work']:.1f} valid pixels of 64, "
           f"{st['bwd_atomics'] / st['bwd_work']:.1f} atomics, all 32 lanes valid in "
