@@ -364,7 +364,9 @@ typedef struct splat_batch {
 
 /* Host: fills the derived fields of views[0..num_views) and b's totals from
  * scene_points[0..num_scenes) (the scenes' Gaussian counts; scene s starts at
- * the sum of the counts before it). */
+ * the sum of the counts before it).  SPLAT_ERR_OVERFLOW when the scenes hold
+ * more than 2^31 - 1 Gaussians in total or the views more than 2^31 - 1
+ * entries or tiles (Gaussian ids, entries and tiles are int32 on the device). */
 SPLAT_API int splat_batch_layout(splat_batch *b, splat_view *views, const uint32_t *scene_points);
 
 /* Projection forward of every entry (forward.cu:13-131 per view; tile counts

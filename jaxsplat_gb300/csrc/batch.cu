@@ -245,6 +245,10 @@ int splat_batch_layout(splat_batch *b, splat_view *views, const uint32_t *scene_
         return fail(SPLAT_ERR_INVALID_ARG, "block_width must be in [2, 16], got %u", b->block_width);
     unsigned long long gauss = 0;
     for (uint32_t s = 0; s < b->num_scenes; ++s) gauss += scene_points[s];
+    // Gaussian ids (the sorted lists, the records' scene-index tag) are int32
+    if (gauss > 0x7fffffffull)
+        return fail(SPLAT_ERR_OVERFLOW, "scenes hold %llu Gaussians in total, more than 2^31 - 1",
+                    gauss);
     unsigned long long entry = 0, tile = 0, pix = 0;
     for (uint32_t k = 0; k < b->num_views; ++k) {
         splat_view &v = views[k];
