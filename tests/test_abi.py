@@ -146,6 +146,24 @@ def test_invalid_block_width_rejected_without_gpu(lib, bw):
     assert b"block_width" in lib.splat_last_error()
 
 
+@pytest.mark.parametrize("n,shape,bw,msg", [
+    (10, (0, 32), 16, b"image size"),
+    (10, (65535, 65535), 2, b"tiles"),          # 32768^2 tiles > 2^22
+    (2**31, (32, 32), 16, b"exceeds int32"),
+])
+def test_invalid_sizes_rejected_without_gpu(lib, n, shape, bw, msg):
+    """Every typed entry point validates the parameters before any CUDA call:
+    empty images, tile grids past 2^22 tiles, point counts past int32."""
+    from jaxsplat_gb300 import _lib
+
+    p = _lib.make_params(n, shape, block_width=bw)
+    for call in (lambda: lib.splat_project_fwd(C.byref(p), *([None] * 13), None, 0, None),
+                 lambda: lib.splat_rasterize_fwd(C.byref(p), 0, *([None] * 8), None),
+                 lambda: lib.splat_project_bwd(C.byref(p), *([None] * 17), None)):
+        assert call() == 1
+        assert msg in lib.splat_last_error()
+
+
 def test_strings(lib):
     assert lib.splat_status_string(4) == b"intersection count out of range"
     assert b"lookback-timeout" in lib.splat_device_status_string(1)
