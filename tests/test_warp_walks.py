@@ -26,6 +26,7 @@ def test_warp_walk_replay(num_points, img_shape, seed):
     assert 0 < st["fwd_work"] <= st["fwd_walk"]
     assert st["fwd_work"] <= st["fwd_active_lanes"] <= 32 * st["fwd_walk"]
     assert st["tile_contributing"] + st["past_saturation"] <= st["entries"]
+    assert st["tile_contributing"] <= st["bwd_staged"] <= st["entries"]
     hist = st["lanes_hist"]
     assert hist[0] == 0 and hist.sum() == st["bwd_work"]
     assert st["bwd_valid_pixels"] >= st["bwd_work"]

@@ -73,7 +73,7 @@ def _meets(x, y, hx, hy, x0, x1, y0, y1):
 
 
 COUNT_KEYS = ("entries", "tile_contributing", "past_saturation", "fwd_walk", "fwd_work",
-              "fwd_active_lanes", "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics",
+              "fwd_active_lanes", "bwd_staged", "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics",
               "final_idx_mismatch", "box_culled_contributing", "identity_mismatch")
 
 
@@ -121,6 +121,9 @@ def _replay_tile(tot, lanes_hist, lo, hi, ox, oy, h, w, ids, xys, con, opac, ex_
     fid = np.where(inside, fidx_img[np.minimum(pyi, h - 1), np.minimum(pxi, w - 1)], 0)
     tot["final_idx_mismatch"] += int((replay_fidx != fid)[inside].sum())
     rows = np.arange(L)
+    # the backward stages (gathers the records of) every entry up to the
+    # block's largest final_idx
+    tot["bwd_staged"] += min(L, max(0, int(fid[inside].max(initial=0)) - lo + 1))
 
     for wv in range(8):
         x0, y0 = (wv & 1) * 8, (wv >> 1) * 4
@@ -215,7 +218,9 @@ def _main():
     print({k: v for k, v in st.items()})
     print(f"forward iterations that do work:  {st['fwd_work'] / st['fwd_walk']:.3f}; lanes not "
           f"yet saturated per walked iteration: {st['fwd_active_lanes'] / st['fwd_walk']:.1f} of 32")
-    print(f"backward iterations that do work: {st['bwd_work'] / st['bwd_walk']:.3f}")
+    print(f"backward iterations that do work: {st['bwd_work'] / st['bwd_walk']:.3f}; entries "
+          f"staged {st['bwd_staged']}, of which blended somewhere in the tile "
+          f"{st['tile_contributing'] / st['bwd_staged']:.3f}")
     print(f"entries contributing somewhere in their tile: "
           f"{st['tile_contributing'] / st['entries']:.3f}; past the saturation of every pixel "
           f"of their tile: {st['past_saturation'] / st['entries']:.3f}")
