@@ -1113,7 +1113,9 @@ int launch_raster_bwd(const splat_params &p, Count count, const int32_t *ids,
                       const float *v_alpha, float *v_colors, float *v_opac, float *v_xy,
                       float *v_xy_abs, float *v_conic, cudaStream_t s) {
     const size_t n = p.num_points;
-    // outputs are sums: start from zero (lib/ops.cu:534-572)
+    // outputs are sums: start from zero (lib/ops.cu:534-572); with no
+    // Gaussians there is nothing to clear and nothing to rasterize
+    if (n == 0) return SPLAT_OK;
     if (cudaMemsetAsync(v_colors, 0, n * 3 * sizeof(float), s) != cudaSuccess ||
         cudaMemsetAsync(v_opac, 0, n * sizeof(float), s) != cudaSuccess ||
         cudaMemsetAsync(v_xy, 0, n * 2 * sizeof(float), s) != cudaSuccess ||

@@ -201,6 +201,26 @@ def test_all_culled_renders_background():
         assert (out[k] == 0).all(), k
 
 
+def test_no_gaussians_renders_background():
+    """N = 0 through the public render API: the background image, and a
+    backward pass that completes with empty gradients."""
+    import torch
+
+    import jaxsplat_gb300 as js
+
+    dev = "cuda"
+    params = [torch.zeros(0, k, device=dev, requires_grad=True) for k in (3, 3, 4, 3, 1)]
+    bg = torch.tensor([0.25, 0.5, 0.75], device=dev)
+    img = js.render(*params, viewmat=torch.eye(4, device=dev), background=bg, img_shape=(20, 30),
+                    f=(30.0, 30.0), c=(15.0, 10.0), glob_scale=1.0, clip_thresh=0.01)
+    assert tuple(img.shape) == (20, 30, 3)
+    assert torch.equal(img, bg.expand(20, 30, 3))
+    img.sum().backward()
+    torch.cuda.synchronize()
+    for t in params:
+        assert t.grad is None or t.grad.numel() == 0
+
+
 def test_single_gaussian():
     from gpu_pipeline import run_cuda
     from oracle.oracle import Oracle
