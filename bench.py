@@ -51,11 +51,11 @@ UNIT = "ms"
 L2_FLUSH_BYTES = 256 << 20
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# the dominant kernel on the 1M-Gaussian 1920x1080 scene, from the ncu capture
-# summarised in profiles/raster_bwd16_hd.md (104.24 MB read + 5.39 MB written).
+# the dominant kernel on the 1M-Gaussian 1920x1080 scene, from one ncu
+# capture of that launch (104.24 MB read + 5.39 MB written).
 NCU_TRAFFIC = {"raster_bwd": 104_242_176 + 5_385_728}
-# The batched backward captured at a quarter of the batch's Gaussian counts
-# (profiles/kernels_batch_quarter.md): bytes read, bytes written, intersections.
+# The batched backward captured at a quarter of the batch's Gaussian counts:
+# bytes read, bytes written, intersections.
 NCU_BATCH_QUARTER = {"raster_bwd": (1_278_222_080, 106_604_800, 23_673_320)}
 
 

@@ -296,9 +296,13 @@ SPLAT_API int splat_xla_make_descriptor(uint32_t num_points, uint32_t img_h, uin
  * loads it, held until exit).
  *   - at most 16,777,216 Gaussians; larger inputs fail with
  *     SPLAT_ERR_INVALID_ARG before any GPU work;
- *   - uses the calling thread's current device (the stream must belong to
- *     it); the first call on a device looks up the array's device address,
- *     so make that first call before any stream capture;
+ *   - uses the calling thread's current CUDA context: the array's device
+ *     address belongs to that context, so the first call in each context
+ *     (each device's primary context, again after cudaDeviceReset, and any
+ *     context the host creates itself) looks the address up and caches it
+ *     under the context's ID -- make that first call before any stream
+ *     capture; a stream of another context fails with
+ *     SPLAT_ERR_INVALID_ARG before any GPU work;
  *   - all calls on a device share the array: calls that overlap on the GPU
  *     race and must be ordered by the caller; each call clears the part it
  *     uses, so back-to-back calls are fine;

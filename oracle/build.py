@@ -13,7 +13,12 @@
   ref_harness.cu (host code of this repository that loads those cubins and
   repeats lib/ops.cu's orchestration with CUB from the CUDA toolkit).
 
-Usage: ``python oracle/build.py [--ref /path/to/reference]``.
+Usage: ``python oracle/build.py [--ref /path/to/reference]``.  The
+reference sources are looked up in ``--ref``, else in the environment
+variable SPLAT_REFERENCE_DIR, else in REFERENCE_DIR_DEFAULT below (where this
+recipe's build machine keeps the read-only reference checkout).  Machines
+without the sources (the GPU machine) skip the cubin build and use the cubins
+that travelled with the working tree.
 """
 
 from __future__ import annotations
@@ -28,6 +33,13 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 REF_ARCH = ["-gencode", "arch=compute_103,code=sm_103"]
 NVCC = os.environ.get("NVCC", "nvcc")
+REFERENCE_DIR_DEFAULT = "/root/reference"
+
+
+def reference_dir() -> str:
+    """Where the reference sources are read from (SPLAT_REFERENCE_DIR
+    overrides the recipe's default)."""
+    return os.environ.get("SPLAT_REFERENCE_DIR", REFERENCE_DIR_DEFAULT)
 
 
 def _stale(out: str, *srcs: str) -> bool:
@@ -55,7 +67,7 @@ def ref_cubins_present() -> bool:
                for n in ("forward", "backward", "other"))
 
 
-def build_ref_cubins(ref_dir: str = "/root/reference", force: bool = False) -> bool:
+def build_ref_cubins(ref_dir: str, force: bool = False) -> bool:
     lib = os.path.join(ref_dir, "lib")
     if not os.path.isdir(lib):
         return False
@@ -88,12 +100,12 @@ def build_harness(force: bool = False) -> str:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--no-harness", action="store_true")
     a = ap.parse_args()
     build_oracle(a.force)
-    built = build_ref_cubins(a.ref, a.force)
+    built = build_ref_cubins(a.ref or reference_dir(), a.force)
     print("reference cubins:", "built" if built else "skipped (no sources)",
           "present" if ref_cubins_present() else "absent")
     if not a.no_harness and ref_cubins_present():

@@ -32,11 +32,14 @@ def _alloc_outputs(torch, n):
                 total=torch.full((1,), -7, dtype=torch.int64, device="cuda"))
 
 
-def _run(lib, torch, p, inputs, use_noalloc):
+def _run(lib, torch, p, inputs, use_noalloc, with_total=True):
     n = inputs[0].shape[0]
     out = _alloc_outputs(torch, n)
     ptrs = [C.c_void_p(t.data_ptr()) for t in inputs] + \
            [C.c_void_p(out[k].data_ptr()) for k in OUT_KEYS]
+    if not with_total:
+        # no total_out: the total goes to the scratch array's last word
+        ptrs[-1] = None
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     if use_noalloc:
         rc = lib.splat_project_fwd_noalloc(C.byref(p), *ptrs, stream)
@@ -78,3 +81,42 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     rc = lib.splat_project_fwd_noalloc(C.byref(p), *([None] * 13), None)
     assert rc == 1
     assert b"at most 16777216" in lib.splat_last_error()
+
+
+def test_noalloc_without_total_and_without_allocating():
+    """total_out = NULL (the total lands in the library's own scratch), and
+    a call after the first leaves the device's free memory and torch's
+    allocator untouched."""
+    import torch
+
+    from jaxsplat_gb300 import _lib
+    from jaxsplat_gb300.scenes import make_scene
+
+    lib = _lib.load()
+    sc = make_scene("small", seed=5, num_points=50_000, img_shape=(200, 240))
+    kw = sc.kwargs
+    p = _lib.make_params(50_000, kw["img_shape"], kw["f"], kw["c"], kw["glob_scale"],
+                         kw["clip_thresh"], 16)
+    inputs = [torch.from_numpy(getattr(sc, k)).cuda()
+              for k in ("means3d", "scales", "quats", "viewmat")]
+    want = _run(lib, torch, p, inputs, use_noalloc=False)
+    _run(lib, torch, p, inputs, use_noalloc=True, with_total=False)  # first call: set-up
+    n = 50_000
+    out = _alloc_outputs(torch, n)
+    ptrs = [C.c_void_p(t.data_ptr()) for t in inputs] + \
+           [C.c_void_p(out[k].data_ptr()) for k in OUT_KEYS[:-1]] + [None]
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = (torch.cuda.memory_allocated(), torch.cuda.memory_reserved())
+    rc = lib.splat_project_fwd_noalloc(C.byref(p), *ptrs, stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = (torch.cuda.memory_allocated(), torch.cuda.memory_reserved())
+    assert rc == 0, lib.splat_last_error()
+    assert free1 == free0, (free0, free1)
+    assert stats1 == stats0
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    for k in OUT_KEYS[:-1]:
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+    assert int(got["total"][0]) == -7  # untouched: no total_out was given

@@ -23,11 +23,10 @@ The replay checks three facts on realistic lists:
     contributions would give the backward an exact skip list.
 and counts the iterations each warp executes and how many of them do work.
 
-``python tests/warp_walks.py [tiles]`` prints the counts for the 1M-Gaussian
-1920x1080 scene over a seeded sample of its tiles."""
+``walk_stats(scene, tiles=k)`` returns the counts for a seeded sample of k
+tiles of a scene (the figures quoted for the 1M-Gaussian 1920x1080 scene use
+400 tiles of ``make_scene("hd", seed=0)``)."""
 
-import os
-import sys
 
 import numpy as np
 
@@ -205,31 +204,3 @@ def walk_stats(scene, tiles=None, seed=0, few_lanes=16, threads=None):
     tot["tiles"] = int(pick.size)
     tot["lanes_hist"] = hist
     return tot
-
-
-def _main():
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    sys.path.insert(0, root)
-    from jaxsplat_gb300.scenes import make_scene
-
-    tiles = int(sys.argv[1]) if len(sys.argv) > 1 else 400
-    st = walk_stats(make_scene("hd", seed=0), tiles=tiles)
-    hist = st.pop("lanes_hist")
-    print({k: v for k, v in st.items()})
-    print(f"forward iterations that do work:  {st['fwd_work'] / st['fwd_walk']:.3f}; lanes not "
-          f"yet saturated per walked iteration: {st['fwd_active_lanes'] / st['fwd_walk']:.1f} of 32")
-    print(f"backward iterations that do work: {st['bwd_work'] / st['bwd_walk']:.3f}; entries "
-          f"staged {st['bwd_staged']}, of which blended somewhere in the tile "
-          f"{st['tile_contributing'] / st['bwd_staged']:.3f}")
-    print(f"entries contributing somewhere in their tile: "
-          f"{st['tile_contributing'] / st['entries']:.3f}; past the saturation of every pixel "
-          f"of their tile: {st['past_saturation'] / st['entries']:.3f}")
-    print(f"backward, per iteration that does work: "
-          f"{st['bwd_valid_pixels'] / st['bwd_work']:.1f} valid pixels of 64, "
-          f"{st['bwd_atomics'] / st['bwd_work']:.1f} atomics, all 32 lanes valid in "
-          f"{hist[32] / st['bwd_work']:.3f}, per-lane atomics in "
-          f"{hist[:17].sum() / st['bwd_work']:.3f}")
-
-
-if __name__ == "__main__":
-    _main()
