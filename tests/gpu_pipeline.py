@@ -15,8 +15,10 @@ def to_dev(inp: dict) -> dict:
             for k in INPUT_KEYS if k in inp}
 
 
-def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True) -> dict:
-    """project -> sort/bin (with intermediates) -> rasterize fwd [-> bwd chain]."""
+def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True, device=False) -> dict:
+    """project -> sort/bin (with intermediates) -> rasterize fwd [-> bwd chain].
+    Returns numpy arrays, or the CUDA tensors themselves with ``device``;
+    ``v_img`` may be a numpy array or a CUDA tensor."""
     t = to_dev(inp)
     p = _ops.project_fwd(t["means3d"], t["scales"], t["quats"], t["viewmat"], block_width=bw,
                          **kw)
@@ -33,7 +35,8 @@ def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True) -> dict:
     out["count"] = torch.tensor(count)
     if v_img is not None:
         h, w = kw["img_shape"]
-        vi = torch.from_numpy(np.ascontiguousarray(v_img, np.float32)).cuda()
+        vi = (v_img.contiguous() if isinstance(v_img, torch.Tensor)
+              else torch.from_numpy(np.ascontiguousarray(v_img, np.float32)).cuda())
         rb = _ops.rasterize_bwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed,
                                 t["background"], r["final_Ts"], r["final_idx"], vi,
                                 torch.zeros(h, w, 1, device="cuda"), img_shape=kw["img_shape"],
@@ -45,4 +48,6 @@ def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True) -> dict:
         out.update(rb)
         out.update(pb)
     torch.cuda.synchronize()
+    if device:
+        return out
     return {k: v.cpu().numpy() for k, v in out.items()}

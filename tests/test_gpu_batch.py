@@ -1,5 +1,8 @@
 """Batched multi-view, multi-scene render (BatchSession): every view's image,
-final_Ts and final_idx equal the single-view render of that view bit for bit;
+final_Ts and final_idx match the reference's kernels rendering that view
+alone (one call per view, jaxsplat/__init__.py:6-70), and each scene's
+gradients match the sum of the reference's per-view gradients; every view
+also equals this library's single-view render of that view bit for bit;
 per-entry screen-space gradients equal the view's own; scene gradients equal
 the sum over the scene's views of the single-view gradients; graph replay
 equals eager; capacity overflow is reported."""
@@ -7,7 +10,7 @@ equals eager; capacity overflow is reported."""
 import numpy as np
 import pytest
 
-from conftest import normwise_rel
+from conftest import GRAD_RTOL, IMG_ATOL, assert_elementwise, normwise_rel
 
 pytestmark = pytest.mark.gpu
 
@@ -77,6 +80,75 @@ def test_batch_views_match_single_view_renders(bw):
         for name in ("means3d", "scales", "quats", "colors", "opacities"):
             assert normwise_rel(got[name].cpu().numpy(), sums[sc][name]) <= 1e-5, (sc, name)
     assert abs(float(bs.loss.item()) - loss) <= 1e-5 * max(1.0, loss)
+
+
+REF_SIZES = ((128, 128), (90, 160), (108, 192))  # 512^2, 1280x720, 1920x1080 scaled down
+
+
+@pytest.mark.parametrize("bw", [16, 8, 12])
+def test_batch_views_match_reference(bw):
+    """Four scenes of a few thousand Gaussians, two views each, mixed image
+    sizes: the batch against the reference's kernels, one call per view."""
+    import torch
+
+    from oracle import ref
+    from jaxsplat_gb300.batch import BatchSession
+    from jaxsplat_gb300.scenes import make_batch
+
+    if not ref.available():
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    rk = ref.RefKernels()
+    scenes, views, targets = make_batch(11, scene_points=(2000, 3000, 4000, 6000),
+                                        views_per_scene=2, sizes=REF_SIZES)
+    views[3]["background"] = np.array([0.2, 0.5, 0.9], np.float32)
+    bs = BatchSession(scenes, views, targets, block_size=bw)
+    bs.measure_capacity()
+    bs.step()
+    bs.check()
+    lengths = (bs.tile_bins[:, 1] - bs.tile_bins[:, 0]).long()
+    sums = [None] * len(scenes)
+    loss = 0.0
+    bit_identical = True
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()  # noqa: E731
+    for k, v in enumerate(views):
+        sc = scenes[v["scene"]]
+        h, w = v["img_shape"]
+        kw = dict(img_shape=(h, w), f=v["f"], c=v["c"], glob_scale=1.0, clip_thresh=0.01)
+        args = [dev(sc[n]) for n in ("means3d", "scales", "quats", "colors", "opacities")]
+        vm, bg, tgt = dev(v["viewmat"]), dev(v["background"]), dev(targets[k])
+        fwd = rk.render(*args, viewmat=vm, background=bg, block_size=bw, **kw)
+        v_img = (2.0 * (fwd["img"] - tgt) / fwd["img"].numel()).contiguous()
+        r = rk.render(*args, viewmat=vm, background=bg, block_size=bw, v_img=v_img, **kw)
+        loss += float(torch.mean((fwd["img"] - tgt) ** 2))
+        assert int(r["cum_tiles_hit"][-1]) > 0, k
+        img = bs.view_image(k)
+        Ts, idx = bs.view_final(k)
+        for name, a, b in (("img", img, r["img"]), ("final_Ts", Ts, r["final_Ts"])):
+            err = float((a.double() - b.double()).abs().max())
+            assert err <= IMG_ATOL, (k, name, err)
+            bit_identical &= bool(torch.equal(a, b))
+        off = int(lengths[:bs.views_host[k].tile_base].sum())
+        expect = torch.where(r["final_Ts"] < 1.0, r["final_idx"] + off,
+                             torch.zeros_like(r["final_idx"]))
+        assert torch.equal(idx, expect), k
+        e = bs.view_entries(k)
+        for name in ("v_xy", "v_conic"):
+            err = normwise_rel(getattr(bs, name)[e].cpu().numpy(), r[name].cpu().numpy())
+            assert err <= GRAD_RTOL, (k, name, err)
+        g = dict(means3d=r["v_mean3d"], scales=r["v_scale"], quats=r["v_quat"],
+                 colors=r["v_colors"], opacities=r["v_opacity"])
+        g = {n: t.double().cpu().numpy() for n, t in g.items()}
+        sums[v["scene"]] = g if sums[v["scene"]] is None else \
+            {n: sums[v["scene"]][n] + g[n] for n in g}
+    for s in range(len(scenes)):
+        got = bs.scene_grads(s)
+        for name in ("means3d", "scales", "quats", "colors", "opacities"):
+            a = got[name].detach().cpu().numpy()
+            assert normwise_rel(a, sums[s][name]) <= GRAD_RTOL, (s, name)
+            assert_elementwise(a, sums[s][name], f"bw{bw} scene {s} {name}")
+    assert abs(float(bs.loss.item()) - loss) <= 1e-5 * max(1.0, loss)
+    print(f"bw {bw}: every view's image and final_Ts bit-identical to the reference's: "
+          f"{bit_identical}")
 
 
 def test_batch_graph_replay_matches_eager():
