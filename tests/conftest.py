@@ -74,12 +74,12 @@ def normwise_rel(a, b) -> float:
 # whose reference magnitude is at least ELEM_FLOOR x the array's largest, the
 # relative error |a - b| / |b| has its 99th percentile within ELEM_P99 and its
 # maximum within ELEM_MAX.  Two fp32 implementations that sum the same terms
-# in different orders (the reference's atomics, the oracle's loops) differ
-# by a few 1e-6 at the 99th percentile and up to ~1e-3 on the odd entry whose
-# terms cancel.
+# in different orders (the reference's atomics, this library's reductions)
+# were measured at p99 <= 8.2e-6 and max <= 6.8e-4 on every case (100k to 6M
+# Gaussians, batched views, block widths 8-16); the bar keeps ~4x headroom.
 ELEM_FLOOR = 1e-3
-ELEM_P99 = 1e-4
-ELEM_MAX = 1e-2
+ELEM_P99 = 3e-5
+ELEM_MAX = 3e-3
 
 
 def elementwise_rel(a, b, floor: float = ELEM_FLOOR):

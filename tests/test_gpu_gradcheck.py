@@ -6,7 +6,8 @@ kernels (fp32, atomics) on the same inputs and the same loss cotangent.
 Bound on the entries that are not flagged as non-smooth: relative error
 |a - d| / max(|a|, |d|, 1e-3 * max|adjoint|) within CUDA_MAX, where d is the
 Richardson-extrapolated difference (accurate to ~1e-8 where the loss is
-smooth, so what is left is the fp32 arithmetic of the kernels)."""
+smooth, so what is left is the fp32 arithmetic of the kernels).  Measured:
+at most 4.5e-5 over the five groups, median ~2e-6."""
 
 import numpy as np
 import pytest
@@ -15,7 +16,7 @@ from fd_entries import GROUPS, PER_GROUP, compare, fd_table, gradcheck_inputs
 
 pytestmark = pytest.mark.gpu
 
-CUDA_MAX = 1e-2
+CUDA_MAX = 2e-4
 
 
 @pytest.fixture(scope="module")
