@@ -1,10 +1,10 @@
 // raster.cu -- tile rasterizer, forward and backward, and the per-Gaussian
 // packing pass that feeds them.
 //
-// One block per tile, one thread per pixel (bw x bw threads, bw <= 16).
-// Per-pixel arithmetic is the reference's (forward.cu:339-462,
-// backward.cu:153-343), evaluated in the same order so that final_idx and the
-// image are bit-identical; what differs is how the work is organised:
+// One block per tile.  Per-pixel arithmetic is the reference's
+// (forward.cu:339-462, backward.cu:153-343), evaluated in the same order so
+// that final_idx and the image are bit-identical; what differs is how the
+// work is organised:
 //
 //  * pack_kernel turns (xys, conics, colors, opacities) into one 48-byte
 //    record per Gaussian, with a conservative box around the pixels where its
@@ -16,14 +16,17 @@
 //    and walks only those.  The skipped ones are Gaussians that the
 //    reference's per-pixel test (alpha < 1/255) rejects at every pixel of
 //    the warp anyway.
-//    For 16x16 tiles each warp covers an 8x4 pixel block (not two rows), which
-//    makes the rectangles compact and the masks sparse.
+//  * 16x16 tiles (raster_fwd16_kernel, raster_bwd16_kernel): 128 threads,
+//    each warp an 8x8 pixel block, each lane two pixels of one column.  The
+//    two pixels share dx, and their arithmetic runs as paired fp32
+//    instructions (FFMA2/FMUL2/FADD2) that round each component exactly as
+//    the scalar instruction would.  Other widths: one pixel per thread,
+//    row-major (raster_fwd_kernel, raster_bwd_kernel).
 //  * backward: the block starts at the largest final_idx of its pixels;
 //    per-Gaussian sums are reduced across the warp with a transposed butterfly
 //    (9 shuffles for 8 values) when many lanes contribute, or added per lane
 //    when few do, and go to global memory with one atomic per field per
-//    (warp, Gaussian).  For 16x16 tiles a thread handles two pixels (see
-//    raster_bwd16_kernel).
+//    (warp, Gaussian).
 #include <math_constants.h>
 
 #include <algorithm>
@@ -84,41 +87,22 @@ __global__ void __launch_bounds__(256) pack_batch_kernel(PackArgs a, const splat
 // ---------------------------------------------------------------------------
 // Pixel layout and warp rectangles.
 
-// Thread -> pixel of the tile.  16x16 tiles: warp w covers the 8x4 block at
-// ((w & 1) * 8, (w >> 1) * 4); other widths: row-major.
-template <bool k8x4>
+// Thread -> pixel of the tile for the one-pixel-per-thread kernels (tile
+// widths other than 16): row-major.
 __device__ __forceinline__ void pixel_of(int tr, int bw, int &tx, int &ty) {
-    if (k8x4) {
-        const int w = tr >> 5, l = tr & 31;
-        tx = ((w & 1) << 3) | (l & 7);
-        ty = ((w >> 1) << 2) | (l >> 3);
-    } else {
-        tx = tr % bw;
-        ty = tr / bw;
-    }
+    tx = tr % bw;
+    ty = tr / bw;
 }
 
-// Bounding rectangle of the pixel centres of warp w, in image coordinates
-// (x_lo, x_hi, y_lo, y_hi).
-template <bool k8x4>
+// Bounding rectangle of the pixel centres of warp w (row-major pixels), in
+// image coordinates (x_lo, x_hi, y_lo, y_hi).
 __device__ __forceinline__ float4 warp_rect(int w, int bw, int bsize, float ox, float oy) {
-    int x0, x1, y0, y1;
-    if (k8x4) {
-        x0 = (w & 1) * 8;
-        x1 = x0 + 7;
-        y0 = (w >> 1) * 4;
-        y1 = y0 + 3;
-    } else {
-        const int first = 32 * w, last = min(first + 31, bsize - 1);
-        y0 = first / bw;
-        y1 = last / bw;
-        if (y0 == y1) {
-            x0 = first % bw;
-            x1 = last % bw;
-        } else {
-            x0 = 0;
-            x1 = bw - 1;
-        }
+    const int first = 32 * w, last = min(first + 31, bsize - 1);
+    const int y0 = first / bw, y1 = last / bw;
+    int x0 = 0, x1 = bw - 1;
+    if (y0 == y1) {
+        x0 = first % bw;
+        x1 = last % bw;
     }
     return make_float4(ox + (float)x0 + 0.5f, ox + (float)x1 + 0.5f, oy + (float)y0 + 0.5f,
                        oy + (float)y1 + 0.5f);
@@ -247,7 +231,7 @@ __device__ __forceinline__ void tile_l2_sum(const RasterFwdArgs &a, float sq, fl
     }
 }
 
-template <bool k8x4, bool kLoss = false, bool kViewLoss = false>
+template <bool kLoss = false, bool kViewLoss = false>
 __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &c) {
     __shared__ float4 s_r0[kMaxTile];
     __shared__ float4 s_r1[kMaxTile];
@@ -262,7 +246,7 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
     const unsigned wmask = (warp == nwarps - 1 && (bsize & 31)) ? ((1u << (bsize & 31)) - 1u)
                                                                 : 0xffffffffu;
     int tx, ty;
-    pixel_of<k8x4>(tr, a.bw, tx, ty);
+    pixel_of(tr, a.bw, tx, ty);
     const unsigned i = c.oy + ty;
     const unsigned j = c.ox + tx;
     const float px = (float)j + 0.5f;
@@ -287,7 +271,7 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
         if (kLoss) tile_l2_sum(a, sq, inv, bsize);
         return;
     }
-    if (tr < nwarps) s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
+    if (tr < nwarps) s_rect[tr] = warp_rect(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
     const int2 range = a.bins[tile];
     bool done = !inside;
     float T = 1.f;
@@ -386,9 +370,172 @@ __device__ __forceinline__ void fwd_tile(const RasterFwdArgs &a, const TileCtx &
     if (kLoss) tile_l2_sum(a, sq, inv, bsize);
 }
 
-template <bool k8x4, bool kLoss>
+// Pixel centres of the 8x8 block of warp w in the two-pixels-per-thread
+// 16x16 layout (x_lo, x_hi, y_lo, y_hi).
+__device__ __forceinline__ float4 warp_rect16(int w, float ox, float oy) {
+    const float x0 = (float)((w & 1) * 8), y0 = (float)((w >> 1) * 8);
+    return make_float4(ox + x0 + 0.5f, ox + x0 + 7.5f, oy + y0 + 0.5f, oy + y0 + 7.5f);
+}
+
+// Paired fp32 arithmetic (sm_100+ FFMA2/FMUL2/FADD2): one instruction, two
+// independent IEEE operations rounded to nearest.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float hsum(float2 a) { return a.x + a.y; }
+
+// falloff() for one Gaussian at two pixels sharing dx (same roundings per
+// component).
+__device__ __forceinline__ float2 falloff2(float a, float b, float c, float dx, float2 dy) {
+    const float2 cdy2 = mul2(mul2(f2(c), dy), dy);
+    const float2 inner = fma2(f2(__fmul_rn(a, dx)), f2(dx), cdy2);
+    return fma2(f2(__fmul_rn(b, dx)), dy, mul2(f2(0.5f), inner));
+}
+
+// ---------------------------------------------------------------------------
+// Forward for 16x16 tiles: two pixels per thread, in the backward's layout.
+// 128 threads; warp w owns the 8x8 pixel block at ((w & 1) * 8, (w >> 1) * 8),
+// lane l the pixels (x, y) and (x, y + 4) with x = l & 7, y = l >> 3 inside
+// it.  The two pixels share dx, and their falloff, alpha, transmittance and
+// colour updates run as paired fp32 instructions (FFMA2/FMUL2/FADD2), each
+// component rounded exactly as the scalar code rounds it, so the image,
+// final_Ts and final_idx are those of the one-pixel-per-thread kernel bit for
+// bit.  A warp walks its list while any of its pixels is unsaturated;
+// saturated or non-passing pixels run the blend with alpha = 0, which leaves
+// their state unchanged.
+
+constexpr int kF16Threads = 128;
+constexpr int kF16Warps = 4;
+constexpr int kF16Batch = 256;
+
+template <bool kLoss, bool kViewLoss>
+__device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx &c) {
+    __shared__ float4 s_r0[kF16Batch];
+    __shared__ float4 s_r1[kF16Batch];
+    __shared__ float s_blue[kF16Batch];
+    __shared__ unsigned s_mask[kF16Batch];
+    __shared__ float4 s_rect[kF16Warps];
+    __shared__ uint8_t s_list[kF16Warps][kF16Batch];
+    const int tile = c.tile;
+    const int tr = threadIdx.x, lane = tr & 31, warp = tr >> 5;
+    const unsigned j = c.ox + ((warp & 1) << 3) + (lane & 7);
+    const unsigned i0 = c.oy + ((warp >> 1) << 3) + (lane >> 3);
+    const float px = (float)j + 0.5f;
+    const bool in0 = i0 < c.height && j < c.width;
+    const bool in1 = i0 + 4 < c.height && j < c.width;
+    const size_t pix0 = c.pix_base + (size_t)i0 * c.width + j;
+    const size_t pix1 = pix0 + 4 * (size_t)c.width;
+    const float3 bg = c.bg;
+    const float inv = kViewLoss ? 1.f / (3.f * (float)c.width * (float)c.height) : a.inv_count;
+
+    if (a.count.get() == 0) {  // lib/ops.cu:119-127: background image, zero T and index
+        float sq = 0.f;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!(q ? in1 : in0)) continue;
+            const size_t pix = q ? pix1 : pix0;
+            a.final_Ts[pix] = 0.f;
+            a.final_idx[pix] = 0;
+            a.img[3 * pix] = bg.x;
+            a.img[3 * pix + 1] = bg.y;
+            a.img[3 * pix + 2] = bg.z;
+            if (kLoss) sq += pixel_l2(a, pix, inv, bg.x, bg.y, bg.z);
+        }
+        if (kLoss) tile_l2_sum(a, sq, inv, kF16Threads);
+        return;
+    }
+    if (tr < kF16Warps) s_rect[tr] = warp_rect16(tr, (float)c.ox, (float)c.oy);
+    const int2 range = a.bins[tile];
+    const float2 neg_py = make_float2(-((float)i0 + 0.5f), -((float)(i0 + 4) + 0.5f));
+    bool done0 = !in0, done1 = !in1;
+    float2 T = make_float2(1.f, 1.f);
+    float2 acc_r = make_float2(0.f, 0.f), acc_g = acc_r, acc_b = acc_r;
+    int cur0 = 0, cur1 = 0;
+    for (int start = range.x; start < range.y; start += kF16Batch) {
+        // also publishes s_rect
+        if (__syncthreads_count(done0 && done1) >= kF16Threads) break;
+        for (int e = tr; e < kF16Batch; e += kF16Threads) {
+            const int idx = start + e;
+            if (idx < range.y) {
+                const int g = a.ids[idx];
+                if (g >= 0 && g < a.n) {
+                    const float4 r0 = a.rec[3 * (size_t)g];
+                    const float4 r1 = a.rec[3 * (size_t)g + 1];
+                    const float4 r2 = a.rec[3 * (size_t)g + 2];
+                    s_r0[e] = r0;
+                    s_r1[e] = r1;
+                    s_blue[e] = r2.x;
+                    s_mask[e] = warp_mask(r0, r2, s_rect, kF16Warps);
+                } else {  // corrupt list entry: never contributes
+                    raise_status(a.status, DEV_BAD_ID);
+                    s_mask[e] = 0u;
+                }
+            }
+        }
+        __syncthreads();
+        const int n = min(kF16Batch, range.y - start);
+        const int cnt = warp_list(s_mask, 0, n, warp, lane, 0xffffffffu, s_list[warp]);
+        for (int k = 0; k < cnt; ++k) {
+            const int t = s_list[warp][k];
+            const float4 r0 = s_r0[t];
+            const float4 r1 = s_r1[t];
+            const float dx = r0.x - px;
+            const float2 dy = add2(f2(r0.y), neg_py);
+            const float2 sigma = falloff2(r0.z, r0.w, r1.x, dx, dy);
+            const float2 ov = mul2(f2(r1.y), make_float2(__expf(-sigma.x), __expf(-sigma.y)));
+            const float al0 = fminf(0.999f, ov.x), al1 = fminf(0.999f, ov.y);
+            const bool pass0 = !done0 && !(sigma.x < 0.f || al0 < 1.f / 255.f);
+            const bool pass1 = !done1 && !(sigma.y < 0.f || al1 < 1.f / 255.f);
+            if (!__any_sync(0xffffffffu, pass0 || pass1)) {
+                if (__all_sync(0xffffffffu, done0 && done1)) break;
+                continue;
+            }
+            const float2 al = make_float2(pass0 ? al0 : 0.f, pass1 ? al1 : 0.f);
+            const float2 next_T = mul2(T, fma2(al, f2(-1.f), f2(1.f)));  // T (1 - alpha)
+            // a pixel whose next T would fall to 1e-4 stops before this
+            // Gaussian (forward.cu:432-436)
+            const bool stop0 = pass0 && next_T.x <= 1e-4f;
+            const bool stop1 = pass1 && next_T.y <= 1e-4f;
+            const bool bl0 = pass0 && !stop0, bl1 = pass1 && !stop1;
+            const float2 vis = mul2(make_float2(bl0 ? al0 : 0.f, bl1 ? al1 : 0.f), T);
+            acc_r = fma2(f2(r1.z), vis, acc_r);
+            acc_g = fma2(f2(r1.w), vis, acc_g);
+            acc_b = fma2(f2(s_blue[t]), vis, acc_b);
+            T = make_float2(bl0 ? next_T.x : T.x, bl1 ? next_T.y : T.y);
+            if (bl0) cur0 = start + t;
+            if (bl1) cur1 = start + t;
+            done0 |= stop0;
+            done1 |= stop1;
+        }
+    }
+    float sq = 0.f;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        if (!(q ? in1 : in0)) continue;
+        const size_t pix = q ? pix1 : pix0;
+        const float Tq = q ? T.y : T.x;
+        a.final_Ts[pix] = Tq;
+        a.final_idx[pix] = q ? cur1 : cur0;
+        const float r = blend(q ? acc_r.y : acc_r.x, Tq, bg.x);
+        const float g = blend(q ? acc_g.y : acc_g.x, Tq, bg.y);
+        const float b = blend(q ? acc_b.y : acc_b.x, Tq, bg.z);
+        a.img[3 * pix] = r;
+        a.img[3 * pix + 1] = g;
+        a.img[3 * pix + 2] = b;
+        if (kLoss) sq += pixel_l2(a, pix, inv, r, g, b);
+    }
+    if (kLoss) tile_l2_sum(a, sq, inv, kF16Threads);
+}
+
+template <bool kLoss>
+__global__ void __launch_bounds__(kF16Threads) raster_fwd16_kernel(RasterFwdArgs a) {
+    fwd16_tile<kLoss, false>(a, grid_tile(a.tiles_x, 16, a.width, a.height, a.background));
+}
+
+template <bool kLoss>
 __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
-    fwd_tile<k8x4, kLoss>(a, grid_tile(a.tiles_x, a.bw, a.width, a.height, a.background));
+    fwd_tile<kLoss>(a, grid_tile(a.tiles_x, a.bw, a.width, a.height, a.background));
 }
 
 // ---------------------------------------------------------------------------
@@ -462,7 +609,6 @@ __device__ __forceinline__ float *grad_field(const RasterBwdArgs &a, int f, int 
 // entry's own index.
 template <bool kAbs, bool kScene>
 __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &c) {
-    constexpr bool k8x4 = false;  // other tile widths: row-major pixels
     __shared__ float4 s_r0[kMaxTile];
     __shared__ float4 s_r1[kMaxTile];
     __shared__ float s_blue[kMaxTile];
@@ -478,7 +624,7 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
     const int bsize = a.bw * a.bw;
     const int lane = tr & 31, warp = tr >> 5, nwarps = (bsize + 31) >> 5;
     int tx, ty;
-    pixel_of<k8x4>(tr, a.bw, tx, ty);
+    pixel_of(tr, a.bw, tx, ty);
     const unsigned i = c.oy + ty;
     const unsigned j = c.ox + tx;
     const float px = (float)j + 0.5f;
@@ -504,7 +650,7 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
                                                                 : 0xffffffffu;
     const int warp_bin_final = __reduce_max_sync(wmask, bin_final);
     if (lane == 0) s_wmax[warp] = warp_bin_final;
-    if (tr < nwarps) s_rect[tr] = warp_rect<k8x4>(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
+    if (tr < nwarps) s_rect[tr] = warp_rect(tr, a.bw, bsize, (float)c.ox, (float)c.oy);
     __syncthreads();
     int block_max = 0;
     for (int w = 0; w < nwarps; ++w) block_max = max(block_max, s_wmax[w]);
@@ -630,23 +776,27 @@ constexpr int kT16Threads = 128;
 constexpr int kT16Warps = 4;
 constexpr int kT16Batch = 256;
 
-__device__ __forceinline__ float4 warp_rect16(int w, float ox, float oy) {
-    const float x0 = (float)((w & 1) * 8), y0 = (float)((w >> 1) * 8);
-    return make_float4(ox + x0 + 0.5f, ox + x0 + 7.5f, oy + y0 + 0.5f, oy + y0 + 7.5f);
-}
 
-// Per-pixel state of the backward pass (backward.cu:181-211).
+// Per-pixel state of the backward pass (backward.cu:181-211), for the two
+// pixels of a lane: component x is pixel (x, y), component y pixel (x, y + 4).
 // The running color sum S of backward.cu:193 enters the alpha cotangent
 // only as S . v_out, and the background and alpha-image terms only as
 // T_final (v_out_alpha - bg . v_out); both are carried as scalars:
 //   v_alpha = T (c . v_out) + (T_final (v_out_alpha - bg . v_out) - S . v_out) / (1 - alpha)
 // which is the reference's expression regrouped.
-struct BwdPixel {
-    float py;
-    bool inside;
-    int bin_final;
-    float T, sv, kb;  // transmittance, S . v_out, T_final (v_out_alpha - bg . v_out)
-    float3 v_out;
+//
+// The two pixels run the same arithmetic, so it is written with Blackwell's
+// paired fp32 instructions (FFMA2/FMUL2/FADD2 through __ffma2_rn, __fmul2_rn,
+// __fadd2_rn): one instruction issues both pixels' operation, each component
+// rounded exactly as the scalar operation would be.  The falloff keeps the
+// forward's roundings (falloff() in splat_math.cuh), so both passes make the
+// same contribution decisions.
+struct BwdPair {
+    float2 py;
+    bool inside0, inside1;
+    int bin0, bin1;
+    float2 T, sv, kb;  // transmittance, S . v_out, T_final (v_out_alpha - bg . v_out)
+    float2 vx, vy, vz; // v_out
 };
 
 template <bool kAbs, bool kScene>
@@ -669,24 +819,38 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
     if (a.count.get() == 0) return;  // lib/ops.cu:184-186: gradients stay zero
     const size_t npix = (size_t)c.width * c.height;
     const float3 bg = c.bg;
-    BwdPixel P[2];
+    BwdPair P;
+    {
+        float Tf[2], kb[2], vx[2], vy[2], vz[2];
+        bool in[2];
+        int bin[2];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const unsigned i = i0 + 4 * q;
-        P[q].py = (float)i + 0.5f;
-        P[q].inside = i < c.height && j < c.width;
-        // backward.cu:184: out-of-image threads read the last pixel
-        const size_t pix = c.pix_base + min((size_t)i * c.width + j, npix - 1);
-        const float T_final = a.final_Ts[pix];
-        P[q].T = T_final;
-        P[q].sv = 0.f;
-        P[q].bin_final = P[q].inside ? a.final_idx[pix] : 0;
-        const float3 vo = make_float3(a.v_img[3 * pix], a.v_img[3 * pix + 1], a.v_img[3 * pix + 2]);
-        P[q].v_out = vo;
-        P[q].kb = T_final * (a.v_alpha[pix] - (bg.x * vo.x + bg.y * vo.y + bg.z * vo.z));
+        for (int q = 0; q < 2; ++q) {
+            const unsigned i = i0 + 4 * q;
+            in[q] = i < c.height && j < c.width;
+            // backward.cu:184: out-of-image threads read the last pixel
+            const size_t pix = c.pix_base + min((size_t)i * c.width + j, npix - 1);
+            Tf[q] = a.final_Ts[pix];
+            bin[q] = in[q] ? a.final_idx[pix] : 0;
+            vx[q] = a.v_img[3 * pix];
+            vy[q] = a.v_img[3 * pix + 1];
+            vz[q] = a.v_img[3 * pix + 2];
+            kb[q] = Tf[q] * (a.v_alpha[pix] - (bg.x * vx[q] + bg.y * vy[q] + bg.z * vz[q]));
+        }
+        P.py = make_float2((float)i0 + 0.5f, (float)(i0 + 4) + 0.5f);
+        P.inside0 = in[0];
+        P.inside1 = in[1];
+        P.bin0 = bin[0];
+        P.bin1 = bin[1];
+        P.T = make_float2(Tf[0], Tf[1]);
+        P.sv = make_float2(0.f, 0.f);
+        P.kb = make_float2(kb[0], kb[1]);
+        P.vx = make_float2(vx[0], vx[1]);
+        P.vy = make_float2(vy[0], vy[1]);
+        P.vz = make_float2(vz[0], vz[1]);
     }
     const int2 range = a.bins[tile];
-    const int warp_bin_final = __reduce_max_sync(0xffffffffu, max(P[0].bin_final, P[1].bin_final));
+    const int warp_bin_final = __reduce_max_sync(0xffffffffu, max(P.bin0, P.bin1));
     if (lane == 0) s_wmax[warp] = warp_bin_final;
     if (tr < kT16Warps) s_rect[tr] = warp_rect16(tr, (float)c.ox, (float)c.oy);
     __syncthreads();
@@ -694,6 +858,7 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
 #pragma unroll
     for (int w = 0; w < kT16Warps; ++w) block_max = max(block_max, s_wmax[w]);
     const int top = min(range.y - 1, block_max);
+    const float2 neg_py = make_float2(-P.py.x, -P.py.y);
 
     for (int batch_end = top; batch_end >= range.x; batch_end -= kT16Batch) {
         __syncthreads();  // previous batch fully flushed
@@ -728,53 +893,50 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
             const float4 r1 = s_r1[t];
             const float opac = r1.y;
             const float dx = r0.x - px;
-            bool valid[2];
-            float alpha[2], vis[2], dy[2];
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                valid[q] = P[q].inside && (batch_end - t <= P[q].bin_final);
-                dy[q] = r0.y - P[q].py;
-                alpha[q] = 0.f;
-                vis[q] = 0.f;
-                if (valid[q]) {
-                    const float sigma = falloff(r0.z, r0.w, r1.x, dx, dy[q]);
-                    vis[q] = __expf(-sigma);
-                    alpha[q] = fminf(0.99f, opac * vis[q]);
-                    if (sigma < 0.f || alpha[q] < 1.f / 255.f) valid[q] = false;
-                }
-            }
-            const unsigned vmask = __ballot_sync(0xffffffffu, valid[0] || valid[1]);
+            const float2 dy = add2(f2(r0.y), neg_py);
+            const float2 sigma = falloff2(r0.z, r0.w, r1.x, dx, dy);
+            const float vis0 = __expf(-sigma.x), vis1 = __expf(-sigma.y);
+            const float2 ov = mul2(f2(opac), make_float2(vis0, vis1));
+            const float al0 = fminf(0.99f, ov.x), al1 = fminf(0.99f, ov.y);
+            const int back = batch_end - t;
+            const bool valid0 = P.inside0 && back <= P.bin0 && !(sigma.x < 0.f || al0 < 1.f / 255.f);
+            const bool valid1 = P.inside1 && back <= P.bin1 && !(sigma.y < 0.f || al1 < 1.f / 255.f);
+            const unsigned vmask = __ballot_sync(0xffffffffu, valid0 || valid1);
             if (!vmask) continue;
-            float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            float g_op = 0.f, g_ax = 0.f, g_ay = 0.f;
+            // a pixel that does not contribute runs with alpha = vis = 0: its
+            // T and S stay unchanged (1 / (1 - 0) = 1) and every term it adds
+            // is zero
+            const float2 al = make_float2(valid0 ? al0 : 0.f, valid1 ? al1 : 0.f);
+            const float2 vis = make_float2(valid0 ? vis0 : 0.f, valid1 ? vis1 : 0.f);
+            const float2 oma = fma2(al, f2(-1.f), f2(1.f));  // 1 - alpha, one rounding
+            // == 1.f / (1.f - alpha)
+            const float2 ra = make_float2(__frcp_rn(oma.x), __frcp_rn(oma.y));
+            P.T = mul2(P.T, ra);
+            const float2 fac = mul2(al, P.T);
             const float cr = r1.z, cg = r1.w, cb = s_blue[t];
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                if (!valid[q]) continue;
-                BwdPixel &S = P[q];
-                const float ra = __frcp_rn(1.f - alpha[q]);  // == 1.f / (1.f - alpha)
-                S.T *= ra;
-                const float fac = alpha[q] * S.T;
-                g8[G_R] += fac * S.v_out.x;
-                g8[G_G] += fac * S.v_out.y;
-                g8[G_B] += fac * S.v_out.z;
-                const float cv = cr * S.v_out.x + cg * S.v_out.y + cb * S.v_out.z;
-                const float v_a = S.T * cv + (S.kb - S.sv) * ra;
-                S.sv += fac * cv;
-                const float v_sigma = -opac * vis[q] * v_a;
-                const float ddy = dy[q];
-                g8[G_CA] += 0.5f * v_sigma * dx * dx;
-                g8[G_CB] += v_sigma * dx * ddy;
-                g8[G_CC] += 0.5f * v_sigma * ddy * ddy;
-                const float gx = v_sigma * (r0.z * dx + r0.w * ddy);
-                const float gy = v_sigma * (r0.w * dx + r1.x * ddy);
-                g8[G_X] += gx;
-                g8[G_Y] += gy;
-                g_op += vis[q] * v_a;
-                if (kAbs) {
-                    g_ax += fabsf(gx);
-                    g_ay += fabsf(gy);
-                }
+            const float2 cv = fma2(f2(cr), P.vx, fma2(f2(cg), P.vy, mul2(f2(cb), P.vz)));
+            const float2 v_a = fma2(P.T, cv, mul2(fma2(P.sv, f2(-1.f), P.kb), ra));
+            P.sv = fma2(fac, cv, P.sv);
+            const float2 u = mul2(vis, v_a);            // opacity cotangent, per pixel
+            const float2 v_sigma = mul2(f2(-opac), u);  // -opac vis v_alpha
+            const float2 w = mul2(v_sigma, f2(dx));     // v_sigma dx
+            const float2 z = mul2(v_sigma, dy);         // v_sigma dy
+            const float2 gx = fma2(f2(r0.z), w, mul2(f2(r0.w), z));
+            const float2 gy = fma2(f2(r0.w), w, mul2(f2(r1.x), z));
+            float g8[8];
+            g8[G_R] = hsum(mul2(fac, P.vx));
+            g8[G_G] = hsum(mul2(fac, P.vy));
+            g8[G_B] = hsum(mul2(fac, P.vz));
+            g8[G_CA] = hsum(mul2(w, f2(0.5f * dx)));
+            g8[G_CB] = hsum(mul2(w, dy));
+            g8[G_CC] = hsum(mul2(z, mul2(f2(0.5f), dy)));
+            g8[G_X] = hsum(gx);
+            g8[G_Y] = hsum(gy);
+            const float g_op = hsum(u);
+            float g_ax = 0.f, g_ay = 0.f;
+            if (kAbs) {
+                g_ax = fabsf(gx.x) + fabsf(gx.y);
+                g_ay = fabsf(gy.x) + fabsf(gy.y);
             }
             const int g = s_gid[t];
             const int gc = kScene ? s_cidx[t] : g;
@@ -790,7 +952,7 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
                         atomicAdd(&a.v_xy_abs[2 * (size_t)g + 1], say);
                     }
                 }
-            } else if (valid[0] || valid[1]) {
+            } else if (valid0 || valid1) {
 #pragma unroll
                 for (int f = 0; f < 8; ++f) atomicAdd(grad_field(a, f, g, gc), g8[f]);
                 atomicAdd(&a.v_opac[gc], g_op);
@@ -856,9 +1018,15 @@ __device__ __forceinline__ void for_each_work_tile(const BatchTiles &b, unsigned
     }
 }
 
-template <bool k8x4, bool kLoss>
+template <bool kLoss>
 __global__ void __launch_bounds__(kMaxTile, 5) raster_fwd_batch_kernel(RasterFwdArgs a, BatchTiles b) {
-    for_each_work_tile(b, a.bw, [&](const TileCtx &c) { fwd_tile<k8x4, kLoss, kLoss>(a, c); });
+    for_each_work_tile(b, a.bw, [&](const TileCtx &c) { fwd_tile<kLoss, kLoss>(a, c); });
+}
+
+template <bool kLoss>
+__global__ void __launch_bounds__(kF16Threads) raster_fwd16_batch_kernel(RasterFwdArgs a,
+                                                                          BatchTiles b) {
+    for_each_work_tile(b, 16, [&](const TileCtx &c) { fwd16_tile<kLoss, kLoss>(a, c); });
 }
 
 __global__ void __launch_bounds__(kMaxTile) raster_bwd_batch_kernel(RasterBwdArgs a, BatchTiles b) {
@@ -937,18 +1105,18 @@ int launch_batch_raster_fwd(const splat_batch &b, Count count, const int32_t *id
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
     a.target = target; a.v_img = v_img; a.loss = loss; a.inv_count = 0.f;
     const BatchTiles t = batch_tiles(b, order, chunk, next);
-    const int threads = (int)(b.block_width * b.block_width);
+    int threads = (int)(b.block_width * b.block_width);
     int grid = 0;
     auto run = [&](auto kernel) -> int {
         if (int rc = persistent_grid(kernel, threads, &grid)) return rc;
         kernel<<<grid, threads, 0, s>>>(a, t);
         return check_launch("raster_fwd_batch_kernel");
     };
-    if (b.block_width == 16)
-        return fused ? run(raster_fwd_batch_kernel<true, true>)
-                     : run(raster_fwd_batch_kernel<true, false>);
-    return fused ? run(raster_fwd_batch_kernel<false, true>)
-                 : run(raster_fwd_batch_kernel<false, false>);
+    if (b.block_width == 16) {
+        threads = kF16Threads;
+        return fused ? run(raster_fwd16_batch_kernel<true>) : run(raster_fwd16_batch_kernel<false>);
+    }
+    return fused ? run(raster_fwd_batch_kernel<true>) : run(raster_fwd_batch_kernel<false>);
 }
 
 int launch_batch_raster_bwd(const splat_batch &b, Count count, const int32_t *ids,
@@ -1098,11 +1266,11 @@ int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,
     dim3 grid(tiles_x(p), tiles_y(p));
     const unsigned threads = p.block_width * p.block_width;
     if (p.block_width == 16) {
-        if (fused) raster_fwd_kernel<true, true><<<grid, threads, 0, s>>>(a);
-        else raster_fwd_kernel<true, false><<<grid, threads, 0, s>>>(a);
+        if (fused) raster_fwd16_kernel<true><<<grid, kF16Threads, 0, s>>>(a);
+        else raster_fwd16_kernel<false><<<grid, kF16Threads, 0, s>>>(a);
     } else {
-        if (fused) raster_fwd_kernel<false, true><<<grid, threads, 0, s>>>(a);
-        else raster_fwd_kernel<false, false><<<grid, threads, 0, s>>>(a);
+        if (fused) raster_fwd_kernel<true><<<grid, threads, 0, s>>>(a);
+        else raster_fwd_kernel<false><<<grid, threads, 0, s>>>(a);
     }
     return check_launch("raster_fwd_kernel");
 }
