@@ -25,11 +25,11 @@ int launch_pack(const splat_params &, const float *, const float *, const float 
                 float *, cudaStream_t);
 int launch_raster_fwd(const splat_params &, Count, const int32_t *, const int2 *,
                       const float *, const float *, float *, int32_t *, float *, const float *,
-                      float *, float *, cudaStream_t);
+                      float *, float *, uint8_t *, cudaStream_t);
 int launch_raster_bwd(const splat_params &, Count, const int32_t *, const int2 *,
                       const float *, const float *, const float *, const int32_t *,
                       const float *, const float *, float *, float *, float *, float *, float *,
-                      cudaStream_t);
+                      const uint8_t *, cudaStream_t);
 int launch_count_pairs(const splat_params &, Count, const int32_t *, const int2 *, const float *,
                        const int32_t *, unsigned long long *, cudaStream_t);
 
@@ -374,7 +374,7 @@ int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int
     const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
     return launch_raster_fwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
-                             final_Ts, final_idx, out_img, nullptr, nullptr, nullptr,
+                             final_Ts, final_idx, out_img, nullptr, nullptr, nullptr, nullptr,
                              (cudaStream_t)stream);
 }
 
@@ -395,7 +395,7 @@ int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersects, const 
     const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
     return launch_raster_fwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
-                             final_Ts, final_idx, out_img, target, v_img, loss_out,
+                             final_Ts, final_idx, out_img, target, v_img, loss_out, nullptr,
                              (cudaStream_t)stream);
 }
 
@@ -438,7 +438,7 @@ int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects, const int
     return launch_raster_bwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
                              final_Ts, final_idx, v_img, v_img_alpha, v_colors, v_opacity, v_xy,
-                             v_xy_abs, v_conic, (cudaStream_t)stream);
+                             v_xy_abs, v_conic, nullptr, (cudaStream_t)stream);
 }
 
 int splat_project_bwd(const splat_params *p, const float *means3d, const float *scales,

@@ -192,6 +192,11 @@ struct RasterFwdArgs {
     const float *target;
     float *v_img, *loss;
     float inv_count;
+    // Optional (16x16 tiles): one byte per sorted-list slot, bit w set when
+    // some pixel of warp w blended that entry; the backward walks exactly
+    // those entries.  Written for every entry of each batch the tile
+    // processes (all entries up to the tile's largest final_idx).
+    uint8_t *blend;
 };
 
 // The L2 loss terms of one pixel (inside the image); returns its squared error.
@@ -409,8 +414,16 @@ constexpr int kF16Threads = 128;
 constexpr int kF16Warps = 4;
 constexpr int kF16Batch = 256;
 
-template <bool kLoss, bool kViewLoss>
+// The warps that blended each entry of a batch: byte w of word e is set by
+// warp w (plain byte stores, one warp per byte), then packed to bits 0-3.
+__device__ __forceinline__ uint8_t pack_blend_bytes(uint32_t x) {
+    x &= 0x01010101u;
+    return (uint8_t)((x | (x >> 7) | (x >> 14) | (x >> 21)) & 0xFu);
+}
+
+template <bool kLoss, bool kViewLoss, bool kBlend = false>
 __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx &c) {
+    __shared__ uint32_t s_blend[kBlend ? kF16Batch : 1];
     __shared__ float4 s_r0[kF16Batch];
     __shared__ float4 s_r1[kF16Batch];
     __shared__ float s_blue[kF16Batch];
@@ -452,11 +465,23 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
     float2 T = make_float2(1.f, 1.f);
     float2 acc_r = make_float2(0.f, 0.f), acc_g = acc_r, acc_b = acc_r;
     int cur0 = 0, cur1 = 0;
+    int prev_start = 0, prev_n = 0;  // the batch whose blend bytes are pending
+    auto flush_blend = [&]() {
+        for (int e = tr; e < prev_n; e += kF16Threads)
+            a.blend[prev_start + e] = pack_blend_bytes(s_blend[e]);
+    };
     for (int start = range.x; start < range.y; start += kF16Batch) {
-        // also publishes s_rect
-        if (__syncthreads_count(done0 && done1) >= kF16Threads) break;
+        // also publishes s_rect, and orders the previous batch's walk before
+        // its blend bytes are read
+        const int all_done = __syncthreads_count(done0 && done1);
+        if (kBlend) {
+            flush_blend();
+            prev_n = 0;
+        }
+        if (all_done >= kF16Threads) break;
         for (int e = tr; e < kF16Batch; e += kF16Threads) {
             const int idx = start + e;
+            if (kBlend) s_blend[e] = 0u;
             if (idx < range.y) {
                 const int g = a.ids[idx];
                 if (g >= 0 && g < a.n) {
@@ -498,6 +523,10 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
             const bool stop0 = pass0 && next_T.x <= 1e-4f;
             const bool stop1 = pass1 && next_T.y <= 1e-4f;
             const bool bl0 = pass0 && !stop0, bl1 = pass1 && !stop1;
+            if (kBlend) {
+                const unsigned blended = __ballot_sync(0xffffffffu, bl0 || bl1);
+                if (lane == 0 && blended) reinterpret_cast<uint8_t *>(s_blend)[4 * t + warp] = 1;
+            }
             const float2 vis = mul2(make_float2(bl0 ? al0 : 0.f, bl1 ? al1 : 0.f), T);
             acc_r = fma2(f2(r1.z), vis, acc_r);
             acc_g = fma2(f2(r1.w), vis, acc_g);
@@ -508,6 +537,14 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
             done0 |= stop0;
             done1 |= stop1;
         }
+        if (kBlend) {
+            prev_start = start;
+            prev_n = n;
+        }
+    }
+    if (kBlend && prev_n) {
+        __syncthreads();
+        flush_blend();
     }
     float sq = 0.f;
 #pragma unroll
@@ -528,9 +565,10 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
     if (kLoss) tile_l2_sum(a, sq, inv, kF16Threads);
 }
 
-template <bool kLoss>
+template <bool kLoss, bool kBlend>
 __global__ void __launch_bounds__(kF16Threads) raster_fwd16_kernel(RasterFwdArgs a) {
-    fwd16_tile<kLoss, false>(a, grid_tile(a.tiles_x, 16, a.width, a.height, a.background));
+    fwd16_tile<kLoss, false, kBlend>(a, grid_tile(a.tiles_x, 16, a.width, a.height,
+                                                  a.background));
 }
 
 template <bool kLoss>
@@ -594,6 +632,7 @@ struct RasterBwdArgs {
     const int32_t *final_idx;
     const float *v_img, *v_alpha;
     float *v_colors, *v_opac, *v_xy, *v_xy_abs, *v_conic;
+    const uint8_t *blend;  // the forward's blend bytes (16x16 tiles), or null
 };
 
 // Global gradient slot of field f (G_R..G_Y) of list entry g whose colour
@@ -703,7 +742,7 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
             float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             float g_op = 0.f, g_ax = 0.f, g_ay = 0.f;
             if (valid) {
-                const float ra = __frcp_rn(1.f - alpha);  // == 1.f / (1.f - alpha)
+                const float ra = __fdividef(1.f, 1.f - alpha);  // fast reciprocal, as bwd16_tile
                 T *= ra;
                 const float fac = alpha * T;
                 g8[G_R] = fac * v_out.x;
@@ -799,7 +838,7 @@ struct BwdPair {
     float2 vx, vy, vz; // v_out
 };
 
-template <bool kAbs, bool kScene>
+template <bool kAbs, bool kScene, bool kBlend = false>
 __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx &c) {
     __shared__ float4 s_r0[kT16Batch];
     __shared__ float4 s_r1[kT16Batch];
@@ -865,6 +904,13 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
         for (int e = tr; e < kT16Batch; e += kT16Threads) {
             const int idx = batch_end - e;
             if (idx >= range.x) {
+                // with the forward's blend bytes, an entry that no warp
+                // blended is never gathered
+                const unsigned bm = kBlend ? (unsigned)a.blend[idx] : 0u;
+                if (kBlend && bm == 0u) {
+                    s_mask[e] = 0u;
+                    continue;
+                }
                 const int g = a.ids[idx];
                 if (g >= 0 && g < a.n) {
                     const float4 r0 = a.rec[3 * (size_t)g];
@@ -875,7 +921,7 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
                     s_r0[e] = r0;
                     s_r1[e] = r1;
                     s_blue[e] = r2.x;
-                    s_mask[e] = warp_mask(r0, r2, s_rect, kT16Warps);
+                    s_mask[e] = kBlend ? bm : warp_mask(r0, r2, s_rect, kT16Warps);
                 } else {  // corrupt list entry: never contributes, never flushed
                     raise_status(a.status, DEV_BAD_ID);
                     s_gid[e] = 0;
@@ -909,8 +955,11 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
             const float2 al = make_float2(valid0 ? al0 : 0.f, valid1 ? al1 : 0.f);
             const float2 vis = make_float2(valid0 ? vis0 : 0.f, valid1 ? vis1 : 0.f);
             const float2 oma = fma2(al, f2(-1.f), f2(1.f));  // 1 - alpha, one rounding
-            // == 1.f / (1.f - alpha)
-            const float2 ra = make_float2(__frcp_rn(oma.x), __frcp_rn(oma.y));
+            // 1 / (1 - alpha) with the fast reciprocal (<= 2 ulp; the
+            // reference's IEEE division costs several times as many
+            // instructions): the recomputed T and the gradients differ from
+            // the reference's by a few ulp, 1 - alpha lies in [0.01, 1)
+            const float2 ra = make_float2(__fdividef(1.f, oma.x), __fdividef(1.f, oma.y));
             P.T = mul2(P.T, ra);
             const float2 fac = mul2(al, P.T);
             const float cr = r1.z, cg = r1.w, cb = s_blue[t];
@@ -965,9 +1014,10 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
     }
 }
 
-template <bool kAbs>
+template <bool kAbs, bool kBlend>
 __global__ void __launch_bounds__(kT16Threads) raster_bwd16_kernel(RasterBwdArgs a) {
-    bwd16_tile<kAbs, false>(a, grid_tile(a.tiles_x, 16, a.width, a.height, a.background));
+    bwd16_tile<kAbs, false, kBlend>(a, grid_tile(a.tiles_x, 16, a.width, a.height,
+                                                 a.background));
 }
 
 // ---------------------------------------------------------------------------
@@ -1103,7 +1153,7 @@ int launch_batch_raster_fwd(const splat_batch &b, Count count, const int32_t *id
     a.count = count; a.ids = ids; a.bins = bins;
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = nullptr;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
-    a.target = target; a.v_img = v_img; a.loss = loss; a.inv_count = 0.f;
+    a.target = target; a.v_img = v_img; a.loss = loss; a.inv_count = 0.f; a.blend = nullptr;
     const BatchTiles t = batch_tiles(b, order, chunk, next);
     int threads = (int)(b.block_width * b.block_width);
     int grid = 0;
@@ -1139,7 +1189,7 @@ int launch_batch_raster_bwd(const splat_batch &b, Count count, const int32_t *id
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = nullptr;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.v_img = v_img; a.v_alpha = v_alpha;
     a.v_colors = v_colors; a.v_opac = v_opac; a.v_xy = v_xy; a.v_xy_abs = nullptr;
-    a.v_conic = v_conic;
+    a.v_conic = v_conic; a.blend = nullptr;
     const BatchTiles t = batch_tiles(b, order, chunk, next);
     int grid = 0;
     if (b.block_width == 16) {
@@ -1250,14 +1300,14 @@ int launch_count_pairs(const splat_params &p, Count count, const int32_t *ids, c
 int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,
                       const int2 *bins, const float *rec, const float *background,
                       float *final_Ts, int32_t *final_idx, float *img, const float *target,
-                      float *v_img, float *loss, cudaStream_t s) {
+                      float *v_img, float *loss, uint8_t *blend, cudaStream_t s) {
     RasterFwdArgs a;
     a.tiles_x = tiles_x(p); a.width = p.img_width; a.height = p.img_height; a.bw = p.block_width;
     a.n = (int)p.num_points; a.status = p.device_status;
     a.count = count; a.ids = ids; a.bins = bins;
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = background;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.img = img;
-    a.target = target; a.v_img = v_img; a.loss = loss;
+    a.target = target; a.v_img = v_img; a.loss = loss; a.blend = blend;
     const long long npix3 = 3ll * p.img_width * p.img_height;
     a.inv_count = npix3 > 0 ? 1.f / (float)npix3 : 0.f;
     const bool fused = target != nullptr;
@@ -1266,8 +1316,13 @@ int launch_raster_fwd(const splat_params &p, Count count, const int32_t *ids,
     dim3 grid(tiles_x(p), tiles_y(p));
     const unsigned threads = p.block_width * p.block_width;
     if (p.block_width == 16) {
-        if (fused) raster_fwd16_kernel<true><<<grid, kF16Threads, 0, s>>>(a);
-        else raster_fwd16_kernel<false><<<grid, kF16Threads, 0, s>>>(a);
+        if (blend) {
+            if (fused) raster_fwd16_kernel<true, true><<<grid, kF16Threads, 0, s>>>(a);
+            else raster_fwd16_kernel<false, true><<<grid, kF16Threads, 0, s>>>(a);
+        } else {
+            if (fused) raster_fwd16_kernel<true, false><<<grid, kF16Threads, 0, s>>>(a);
+            else raster_fwd16_kernel<false, false><<<grid, kF16Threads, 0, s>>>(a);
+        }
     } else {
         if (fused) raster_fwd_kernel<true><<<grid, threads, 0, s>>>(a);
         else raster_fwd_kernel<false><<<grid, threads, 0, s>>>(a);
@@ -1279,7 +1334,7 @@ int launch_raster_bwd(const splat_params &p, Count count, const int32_t *ids,
                       const int2 *bins, const float *rec, const float *background,
                       const float *final_Ts, const int32_t *final_idx, const float *v_img,
                       const float *v_alpha, float *v_colors, float *v_opac, float *v_xy,
-                      float *v_xy_abs, float *v_conic, cudaStream_t s) {
+                      float *v_xy_abs, float *v_conic, const uint8_t *blend, cudaStream_t s) {
     const size_t n = p.num_points;
     // outputs are sums: start from zero (lib/ops.cu:534-572); with no
     // Gaussians there is nothing to clear and nothing to rasterize
@@ -1298,13 +1353,18 @@ int launch_raster_bwd(const splat_params &p, Count count, const int32_t *ids,
     a.rec = reinterpret_cast<const float4 *>(rec); a.background = background;
     a.final_Ts = final_Ts; a.final_idx = final_idx; a.v_img = v_img; a.v_alpha = v_alpha;
     a.v_colors = v_colors; a.v_opac = v_opac; a.v_xy = v_xy; a.v_xy_abs = v_xy_abs;
-    a.v_conic = v_conic;
+    a.v_conic = v_conic; a.blend = blend;
     dim3 grid(tiles_x(p), tiles_y(p));
     const unsigned threads = p.block_width * p.block_width;
     const bool wide = p.block_width == 16;
     if (wide) {
-        if (v_xy_abs) raster_bwd16_kernel<true><<<grid, kT16Threads, 0, s>>>(a);
-        else raster_bwd16_kernel<false><<<grid, kT16Threads, 0, s>>>(a);
+        if (blend) {
+            if (v_xy_abs) raster_bwd16_kernel<true, true><<<grid, kT16Threads, 0, s>>>(a);
+            else raster_bwd16_kernel<false, true><<<grid, kT16Threads, 0, s>>>(a);
+        } else {
+            if (v_xy_abs) raster_bwd16_kernel<true, false><<<grid, kT16Threads, 0, s>>>(a);
+            else raster_bwd16_kernel<false, false><<<grid, kT16Threads, 0, s>>>(a);
+        }
         return check_launch("raster_bwd16_kernel");
     }
     if (v_xy_abs)

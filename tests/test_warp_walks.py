@@ -1,8 +1,8 @@
 """The 16x16 rasterizers' warp walks, replayed on the CPU over every tile of
 small scenes (tests/warp_walks.py): the replayed forward reproduces the
 oracle's final_idx, the culling box never drops a contributing pair, and each
-backward warp's entries with a valid pixel are exactly the entries its two
-forward warps blended."""
+backward warp's entries with a valid pixel are exactly the entries the same
+warp blended in the forward."""
 
 import numpy as np
 import pytest
@@ -24,7 +24,7 @@ def test_warp_walk_replay(num_points, img_shape, seed):
     assert st["identity_mismatch"] == 0
     assert 0 < st["bwd_work"] <= st["bwd_walk"]
     assert 0 < st["fwd_work"] <= st["fwd_walk"]
-    assert st["fwd_work"] <= st["fwd_active_lanes"] <= 32 * st["fwd_walk"]
+    assert st["fwd_work"] <= st["fwd_active_pixels"] <= 64 * st["fwd_walk"]
     assert st["tile_contributing"] + st["past_saturation"] <= st["entries"]
     assert st["tile_contributing"] <= st["bwd_staged"] <= st["entries"]
     hist = st["lanes_hist"]

@@ -1,14 +1,13 @@
 """CPU replay of how the 16x16 rasterizers walk a tile's list, on the oracle's
 projection, sorted lists and final_idx (test infrastructure).
 
-Warp layouts (jaxsplat_gb300/csrc/raster.cu, pixel_of and warp_rect16):
-  forward:  8 warps of 8x4 pixels, warp w at ((w & 1) * 8, (w >> 1) * 4); a warp
-            walks the batch entries whose culling box meets its rectangle until
-            every one of its lanes has saturated;
-  backward: 4 warps of 8x8 pixels, warp W at ((W & 1) * 8, (W >> 1) * 8); lane l
-            holds pixels (l & 7, l >> 3) and (l & 7, (l >> 3) + 4); a warp walks
-            the entries up to its largest final_idx whose box meets its
-            rectangle.
+Warp layout (jaxsplat_gb300/csrc/raster.cu, fwd16_tile and bwd16_tile), the
+same in both passes: 4 warps of 8x8 pixels, warp w at ((w & 1) * 8, (w >> 1) * 8);
+lane l holds pixels (l & 7, l >> 3) and (l & 7, (l >> 3) + 4).
+  forward:  a warp walks the batch entries whose culling box meets its
+            rectangle until every one of its pixels has saturated;
+  backward: a warp walks the entries up to its largest final_idx whose box
+            meets its rectangle.
 An iteration "does work" when at least one lane passes the pixel test
 (sigma >= 0, alpha >= 1/255; in the backward also idx <= the pixel's
 final_idx, backward.cu:240-265).
@@ -17,10 +16,10 @@ The replay checks three facts on realistic lists:
   * the replayed forward gives the oracle's final_idx at every pixel;
   * no pair that contributes lies outside the culling box of write_record
     (splat_math.cuh), so the box never changes a result;
-  * per backward warp, the entries with a valid pixel are exactly the
-    entries that contributed (were blended) at some pixel of the two forward
-    warps covering the same 8x8 block: a forward that records its per-warp
-    contributions would give the backward an exact skip list.
+  * per warp, the entries with a valid pixel in the backward are exactly the
+    entries the same warp blended at some pixel in the forward: the blend
+    bytes the forward records (one bit per warp and entry) are an exact skip
+    list for the backward.
 and counts the iterations each warp executes and how many of them do work.
 
 ``walk_stats(scene, tiles=k)`` returns the counts for a seeded sample of k
@@ -72,7 +71,7 @@ def _meets(x, y, hx, hy, x0, x1, y0, y1):
 
 
 COUNT_KEYS = ("entries", "tile_contributing", "past_saturation", "fwd_walk", "fwd_work",
-              "fwd_active_lanes", "bwd_staged", "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics",
+              "fwd_active_pixels", "bwd_staged", "bwd_walk", "bwd_work", "bwd_valid_pixels", "bwd_atomics",
               "final_idx_mismatch", "box_culled_contributing", "identity_mismatch")
 
 
@@ -124,18 +123,18 @@ def _replay_tile(tot, lanes_hist, lo, hi, ox, oy, h, w, ids, xys, con, opac, ex_
     # block's largest final_idx
     tot["bwd_staged"] += min(L, max(0, int(fid[inside].max(initial=0)) - lo + 1))
 
-    for wv in range(8):
-        x0, y0 = (wv & 1) * 8, (wv >> 1) * 4
-        sel = (kx >= x0) & (kx < x0 + 8) & (ky >= y0) & (ky < y0 + 4)
+    for wv in range(4):
+        x0, y0 = (wv & 1) * 8, (wv >> 1) * 8
+        sel = (kx >= x0) & (kx < x0 + 8) & (ky >= y0) & (ky < y0 + 8)
         mb = _meets(gx, gy, ex, ey, f32(ox + x0 + 0.5), f32(ox + x0 + 7.5), f32(oy + y0 + 0.5),
-                    f32(oy + y0 + 3.5))
-        lane_done = np.where(inside[sel], done_at[sel], -1)
-        walk = mb & (rows <= lane_done.max())
-        still = rows[:, None] <= lane_done[None, :]
+                    f32(oy + y0 + 7.5))
+        pix_done = np.where(inside[sel], done_at[sel], -1)
+        walk = mb & (rows <= pix_done.max())
+        still = rows[:, None] <= pix_done[None, :]
         tot["fwd_walk"] += int(walk.sum())
         tot["fwd_work"] += int((walk & (passes[:, sel] & still).any(axis=1)).sum())
-        # lanes not yet saturated (inside the image) in each walked iteration
-        tot["fwd_active_lanes"] += int((still & inside[sel][None, :])[walk].sum())
+        # pixels not yet saturated (inside the image) in each walked iteration
+        tot["fwd_active_pixels"] += int((still & inside[sel][None, :])[walk].sum())
 
     for W in range(4):
         x0, y0 = (W & 1) * 8, (W >> 1) * 8
