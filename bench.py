@@ -702,7 +702,8 @@ WARM_METRIC = "time to 30 dB PSNR, learned init vs plain, 512x512 procedural, N=
 def main_warmstart(a, torch, dev):
     """--scene warmstart: dataset from the plain loop, network training, and
     wall-clock to 30 dB from the network's proposal vs from random init on
-    held-out seeds (value = mean learned seconds; plain alongside)."""
+    held-out seeds (value = mean learned seconds; plain and the mean-proposal
+    ablation alongside)."""
     from jaxsplat_gb300.warmstart import run_experiment
 
     res = run_experiment(n_train=a.ws_train_sets, fit_steps=a.ws_fit_steps, epochs=a.ws_epochs,
@@ -711,8 +712,11 @@ def main_warmstart(a, torch, dev):
     ok = all(r["learned_reached"] and r["plain_reached"] for r in ev)
     learned = float(np.mean([r["learned_s"] for r in ev]))
     plain = float(np.mean([r["plain_s"] for r in ev]))
+    mean = float(np.mean([r["mean_s"] for r in ev]))
+    ok_mean = all(r["mean_reached"] for r in ev)
     print(json.dumps({"metric": WARM_METRIC, "value": round(learned, 4) if ok else None,
                       "unit": "s", "plain_value": round(plain, 4) if ok else None,
+                      "mean_proposal_value": round(mean, 4) if ok_mean else None,
                       "n_gpus": 1, "steps": len(ev), "warmup": 1, "higher_is_better": False,
                       "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, f32 render",
                       "data": "synthetic (procedural targets, seeded; training sets fitted here)",

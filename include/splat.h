@@ -173,12 +173,20 @@ SPLAT_API int splat_pack_splats(const splat_params *p, const float *xys, const f
  * (lib/ops.cu:119-127: image = background, final_Ts = final_idx = 0).
  * num_intersects / count_dev as for splat_sort_and_bin.
  *   packed (N,12) from splat_pack_splats, background (3,)
- *   -> final_Ts (H,W,1) final_idx (H,W,1) int32 out_img (H,W,3) */
+ *   -> final_Ts (H,W,1) final_idx (H,W,1) int32 out_img (H,W,3)
+ *   blend_out (optional, block_width 16; ignored for other widths): one
+ *     byte per sorted-list slot (num_intersects, or the capacity with
+ *     count_dev), bit w set when some pixel of the tile's warp w (the 8x8
+ *     pixel block at ((w & 1) * 8, (w >> 1) * 8)) passed that entry's alpha
+ *     test.  Written for the entries up to the tile's largest final_idx;
+ *     pass it to splat_rasterize_bwd, which then walks only those entries
+ *     (no counterpart in the reference; NULL: not recorded). */
 SPLAT_API int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects,
                                   const int64_t *count_dev,
                                   const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
                                   const float *packed, const float *background, float *final_Ts,
-                                  int32_t *final_idx, float *out_img, splat_stream_t stream);
+                                  int32_t *final_idx, float *out_img, uint8_t *blend_out,
+                                  splat_stream_t stream);
 
 /* splat_rasterize_fwd with the L2 loss of splat_l2_loss fused into its
  * epilogue (each pixel's colour is still in registers): additionally
@@ -192,7 +200,8 @@ SPLAT_API int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersec
                                      const int32_t *tile_bins, const float *packed,
                                      const float *background, const float *target,
                                      float *final_Ts, int32_t *final_idx, float *out_img,
-                                     float *v_img, float *loss_out, splat_stream_t stream);
+                                     float *v_img, float *loss_out, uint8_t *blend_out,
+                                     splat_stream_t stream);
 
 /* Rasterize backward over the same sorted list (no re-sort).  Replaces the
  * rasterize_bwd launch of ops::rasterize::bwd::xla (lib/ops.cu:203-225,
@@ -200,7 +209,11 @@ SPLAT_API int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersec
  *   v_img (H,W,3) v_img_alpha (H,W,1)
  *   -> v_colors (N,3) v_opacity (N,1) v_xy (N,2) v_conic (N,3)
  *      v_xy_abs (N,2) optional: NULL skips the sum of |v_xy| that the
- *      reference computes and jaxsplat discards. */
+ *      reference computes and jaxsplat discards.
+ *   blend (optional, block_width 16): the forward's blend_out over the same
+ *     list; the backward then stages and walks only the entries some pixel
+ *     of each warp passed (same results; NULL: every entry whose culling
+ *     box meets the warp's pixels). */
 SPLAT_API int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
                                   const int64_t *count_dev,
                                   const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
@@ -208,7 +221,7 @@ SPLAT_API int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
                                   const float *final_Ts, const int32_t *final_idx,
                                   const float *v_img, const float *v_img_alpha, float *v_colors,
                                   float *v_opacity, float *v_xy, float *v_xy_abs, float *v_conic,
-                                  splat_stream_t stream);
+                                  const uint8_t *blend, splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Projection backward.  Replaces ops::project::bwd::xla (lib/ops.cu:63-105,
@@ -461,8 +474,8 @@ SPLAT_API int splat_batch_project_bwd(const splat_batch *b, const float *means3d
                                       float *v_scale, float *v_quat, splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
-/* BF16 GEMM on the tensor cores (tcgen05, FP32 accumulation) for the
- * warm-start network; no counterpart in the reference.
+/* BF16 GEMM on the tensor cores (tcgen05 MMA, TMA operand loads, FP32
+ * accumulation) for the warm-start network; no counterpart in the reference.
  *   C[M,N] fp32 row-major (ldc) = A[M,K] x B[N,K]^T (+ C when accumulate),
  *   A, B bf16 row-major (K contiguous; lda, ldb elements), 16-byte aligned,
  *   K, lda, ldb multiples of 8.  status_dev (optional device uint32) gets
@@ -470,6 +483,14 @@ SPLAT_API int splat_batch_project_bwd(const splat_batch *b, const float *means3d
 SPLAT_API int splat_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int lda,
                               int ldb, int ldc, int accumulate, uint32_t *status_dev,
                               splat_stream_t stream);
+/* The same product with the bias, the activation and the output conversion
+ * in the GEMM's epilogue (the fp32 product is never stored):
+ *   y[M,N] = act(A[M,K] x B[N,K]^T + bias[N]), act = ReLU when relu != 0,
+ *   written to exactly one of y16 (bf16) or y32 (fp32), row stride ldy.
+ * K > 0; operand rules as splat_gemm_bf16. */
+SPLAT_API int splat_gemm_bf16_bias_act(const void *A, const void *B, const float *bias, void *y16,
+                                       float *y32, int M, int N, int K, int lda, int ldb, int ldy,
+                                       int relu, uint32_t *status_dev, splat_stream_t stream);
 
 /* Kernels around the GEMM for the warm-start network's 3x3 convolutions
  * (padding 1, stride 1 or 2) on NHWC bf16 activations; no counterpart in the

@@ -84,9 +84,9 @@ _SIGS = [
     ("splat_sort_workspace_size", C.c_size_t, [_P, C.c_int64]),
     ("splat_sort_and_bin", C.c_int, [_P, C.c_int64] + [_v] * 10 + [_v, C.c_size_t, _v]),
     ("splat_pack_splats", C.c_int, [_P] + [_v] * 5 + [_v]),
-    ("splat_rasterize_fwd", C.c_int, [_P, C.c_int64] + [_v] * 8 + [_v]),
-    ("splat_rasterize_fwd_l2", C.c_int, [_P, C.c_int64] + [_v] * 11 + [_v]),
-    ("splat_rasterize_bwd", C.c_int, [_P, C.c_int64] + [_v] * 14 + [_v]),
+    ("splat_rasterize_fwd", C.c_int, [_P, C.c_int64] + [_v] * 9 + [_v]),
+    ("splat_rasterize_fwd_l2", C.c_int, [_P, C.c_int64] + [_v] * 12 + [_v]),
+    ("splat_rasterize_bwd", C.c_int, [_P, C.c_int64] + [_v] * 15 + [_v]),
     ("splat_project_bwd", C.c_int, [_P] + [_v] * 17 + [_v]),
     ("splat_l2_loss", C.c_int, [_v, _v, C.c_int64, _v, _v, _v]),
     ("splat_count_pairs", C.c_int, [_P, C.c_int64] + [_v] * 6 + [_v]),
@@ -118,6 +118,7 @@ _SIGS = [
     ("splat_batch_l2_loss", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 4 + [_v]),
     ("splat_batch_project_bwd", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 12 + [_v]),
     ("splat_gemm_bf16", C.c_int, [_v, _v, _v] + [C.c_int] * 7 + [_v, _v]),
+    ("splat_gemm_bf16_bias_act", C.c_int, [_v] * 5 + [C.c_int] * 7 + [_v, _v]),
     ("splat_nn_im2col3x3", C.c_int, [_v, _v] + [C.c_int] * 6 + [_v]),
     ("splat_nn_col2im3x3", C.c_int, [_v, _v] + [C.c_int] * 6 + [_v]),
     ("splat_nn_bias_act", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),

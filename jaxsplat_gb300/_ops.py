@@ -189,8 +189,9 @@ def pack_splats(xys, conics, colors, opacities, *, img_shape, block_width):
 
 
 def rasterize_fwd(num_intersects, ids_sorted, tile_bins, packed, background, *, img_shape,
-                  block_width, count_dev=None):
-    """lib/ops.cu:144-160 over a sorted list -> dict(final_Ts, final_idx, img)."""
+                  block_width, count_dev=None, blend=False):
+    """lib/ops.cu:144-160 over a sorted list -> dict(final_Ts, final_idx, img)
+    [+ blend: the per-slot warp bytes for rasterize_bwd, block width 16]."""
     lib = _lib.load()
     n = packed.shape[0]
     dev = packed.device
@@ -199,11 +200,13 @@ def rasterize_fwd(num_intersects, ids_sorted, tile_bins, packed, background, *, 
     out = dict(final_Ts=torch.empty(h, w, 1, dtype=torch.float32, device=dev),
                final_idx=torch.empty(h, w, 1, dtype=torch.int32, device=dev),
                img=torch.empty(h, w, 3, dtype=torch.float32, device=dev))
+    if blend and block_width == 16:
+        out["blend"] = torch.empty(max(1, ids_sorted.numel()), dtype=torch.uint8, device=dev)
     args = [_contig(t) for t in (ids_sorted, tile_bins, packed, background)]
     rc = lib.splat_rasterize_fwd(C.byref(p), num_intersects, _ptr(count_dev),
                                  *[_ptr(t) for t in args],
                                  _ptr(out["final_Ts"]), _ptr(out["final_idx"]), _ptr(out["img"]),
-                                 _stream())
+                                 _ptr(out.get("blend")), _stream())
     _lib.check(rc, "rasterize_fwd")
     return out
 
@@ -227,16 +230,17 @@ def rasterize_fwd_l2(num_intersects, ids_sorted, tile_bins, packed, background, 
     rc = lib.splat_rasterize_fwd_l2(C.byref(p), num_intersects, _ptr(count_dev),
                                     *[_ptr(t) for t in args], _ptr(out["final_Ts"]),
                                     _ptr(out["final_idx"]), _ptr(out["img"]), _ptr(out["v_img"]),
-                                    _ptr(out["loss"]), _stream())
+                                    _ptr(out["loss"]), None, _stream())
     _lib.check(rc, "rasterize_fwd_l2")
     return out
 
 
 def rasterize_bwd(num_intersects, ids_sorted, tile_bins, packed, background, final_Ts,
                   final_idx, v_img, v_img_alpha, *, img_shape, block_width, with_abs=False,
-                  count_dev=None):
+                  count_dev=None, blend=None):
     """lib/ops.cu:203-225 over the stored sorted list -> dict(v_colors,
-    v_opacity, v_xy, v_conic[, v_xy_abs])."""
+    v_opacity, v_xy, v_conic[, v_xy_abs]); `blend`: the forward's per-slot
+    warp bytes (rasterize_fwd(..., blend=True)), or None."""
     lib = _lib.load()
     n = packed.shape[0]
     dev = packed.device
@@ -251,7 +255,8 @@ def rasterize_bwd(num_intersects, ids_sorted, tile_bins, packed, background, fin
     rc = lib.splat_rasterize_bwd(C.byref(p), num_intersects, _ptr(count_dev),
                                  *[_ptr(t) for t in args],
                                  _ptr(out["v_colors"]), _ptr(out["v_opacity"]), _ptr(out["v_xy"]),
-                                 _ptr(out.get("v_xy_abs")), _ptr(out["v_conic"]), _stream())
+                                 _ptr(out.get("v_xy_abs")), _ptr(out["v_conic"]), _ptr(blend),
+                                 _stream())
     _lib.check(rc, "rasterize_bwd")
     return out
 
@@ -301,8 +306,9 @@ class ProjectFn(torch.autograd.Function):
 
 class RasterizeFn(torch.autograd.Function):
     """custom_vjp of jaxsplat/_rasterize/__init__.py:71-190.  The sorted
-    intersection list and the packed records are kept as residuals, so the
-    backward does not re-emit and re-sort (lib/ops.cu:188-198 does)."""
+    intersection list, the packed records and (block width 16) the forward's
+    per-slot warp bytes are kept as residuals, so the backward does not
+    re-emit and re-sort (lib/ops.cu:188-198 does)."""
 
     @staticmethod
     def forward(ctx, colors, opacities, background, xys, depths, radii, conics, cum_tiles_hit,
@@ -312,25 +318,26 @@ class RasterizeFn(torch.autograd.Function):
         s = sort_and_bin(count, xys, depths, radii, cum_tiles_hit, **kw)
         packed = pack_splats(xys, conics, colors, opacities, **kw)
         r = rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed, background,
-                          **kw)
+                          blend=True, **kw)
         ctx.kw = kw
         ctx.count = count
+        blend = r.get("blend", torch.empty(0, dtype=torch.uint8, device=colors.device))
         ctx.save_for_backward(packed, background, r["final_Ts"], r["final_idx"],
-                              s["gaussian_ids_sorted"], s["tile_bins"])
+                              s["gaussian_ids_sorted"], s["tile_bins"], blend)
         ctx.mark_non_differentiable(r["final_idx"])
         img_alpha = 1.0 - r["final_Ts"]  # jaxsplat/_rasterize/__init__.py:136
         return r["img"], img_alpha, r["final_idx"]
 
     @staticmethod
     def backward(ctx, v_img, v_img_alpha, _fi):
-        packed, background, final_Ts, final_idx, ids, bins = ctx.saved_tensors
+        packed, background, final_Ts, final_idx, ids, bins, blend = ctx.saved_tensors
         h, w = ctx.kw["img_shape"]
         if v_img is None:
             v_img = torch.zeros(h, w, 3, dtype=torch.float32, device=packed.device)
         if v_img_alpha is None:  # render() drops the alpha image: zero cotangent
             v_img_alpha = torch.zeros(h, w, 1, dtype=torch.float32, device=packed.device)
         g = rasterize_bwd(ctx.count, ids, bins, packed, background, final_Ts, final_idx, v_img,
-                          v_img_alpha, **ctx.kw)
+                          v_img_alpha, blend=blend if blend.numel() else None, **ctx.kw)
         # jaxsplat/_rasterize/__init__.py:187
         return (g["v_colors"], g["v_opacity"], None, g["v_xy"], None, None, g["v_conic"], None,
                 None, None)

@@ -362,7 +362,8 @@ int splat_pack_splats(const splat_params *p, const float *xys, const float *coni
 int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
                         const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
                         const float *packed, const float *background, float *final_Ts,
-                        int32_t *final_idx, float *out_img, splat_stream_t stream) {
+                        int32_t *final_idx, float *out_img, uint8_t *blend_out,
+                        splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     if (int rc = check_count(num_intersects)) return rc;
     NEED(background); NEED(final_Ts); NEED(final_idx); NEED(out_img);
@@ -374,15 +375,15 @@ int splat_rasterize_fwd(const splat_params *p, int64_t num_intersects, const int
     const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
     return launch_raster_fwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
-                             final_Ts, final_idx, out_img, nullptr, nullptr, nullptr, nullptr,
-                             (cudaStream_t)stream);
+                             final_Ts, final_idx, out_img, nullptr, nullptr, nullptr,
+                             p->block_width == 16 ? blend_out : nullptr, (cudaStream_t)stream);
 }
 
 int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
                            const int32_t *gaussian_ids_sorted, const int32_t *tile_bins,
                            const float *packed, const float *background, const float *target,
                            float *final_Ts, int32_t *final_idx, float *out_img, float *v_img,
-                           float *loss_out, splat_stream_t stream) {
+                           float *loss_out, uint8_t *blend_out, splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     if (int rc = check_count(num_intersects)) return rc;
     NEED(background); NEED(target); NEED(final_Ts); NEED(final_idx); NEED(out_img);
@@ -395,8 +396,8 @@ int splat_rasterize_fwd_l2(const splat_params *p, int64_t num_intersects, const 
     const Count c{reinterpret_cast<const long long *>(count_dev), num_intersects, num_intersects};
     return launch_raster_fwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
-                             final_Ts, final_idx, out_img, target, v_img, loss_out, nullptr,
-                             (cudaStream_t)stream);
+                             final_Ts, final_idx, out_img, target, v_img, loss_out,
+                             p->block_width == 16 ? blend_out : nullptr, (cudaStream_t)stream);
 }
 
 int splat_count_pairs(const splat_params *p, int64_t num_intersects, const int64_t *count_dev,
@@ -422,7 +423,7 @@ int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects, const int
                         const float *packed, const float *background, const float *final_Ts,
                         const int32_t *final_idx, const float *v_img, const float *v_img_alpha,
                         float *v_colors, float *v_opacity, float *v_xy, float *v_xy_abs,
-                        float *v_conic, splat_stream_t stream) {
+                        float *v_conic, const uint8_t *blend, splat_stream_t stream) {
     if (int rc = validate(p)) return rc;
     if (int rc = check_count(num_intersects)) return rc;
     if (p->num_points > 0) {
@@ -438,7 +439,8 @@ int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects, const int
     return launch_raster_bwd(*p, c, gaussian_ids_sorted,
                              reinterpret_cast<const int2 *>(tile_bins), packed, background,
                              final_Ts, final_idx, v_img, v_img_alpha, v_colors, v_opacity, v_xy,
-                             v_xy_abs, v_conic, nullptr, (cudaStream_t)stream);
+                             v_xy_abs, v_conic, p->block_width == 16 ? blend : nullptr,
+                             (cudaStream_t)stream);
 }
 
 int splat_project_bwd(const splat_params *p, const float *means3d, const float *scales,
@@ -588,7 +590,8 @@ void splat_xla_rasterize_fwd(splat_stream_t stream, void **b, const char *opaque
         rc = xla_sorted(p, b, s, L);
         if (rc == SPLAT_OK)
             rc = splat_rasterize_fwd(&p, L.count, nullptr, L.ids, L.bins, L.packed, (const float *)b[2],
-                                     (float *)b[8], (int32_t *)b[9], (float *)b[10], stream);
+                                     (float *)b[8], (int32_t *)b[9], (float *)b[10], nullptr,
+                                     stream);
         xla_release(L, s);
     }
     report("rasterize_fwd", rc);
@@ -606,7 +609,7 @@ void splat_xla_rasterize_bwd(splat_stream_t stream, void **b, const char *opaque
                                      (const float *)b[8], (const int32_t *)b[9],
                                      (const float *)b[10], (const float *)b[11], (float *)b[12],
                                      (float *)b[13], (float *)b[14], (float *)b[15],
-                                     (float *)b[16], stream);
+                                     (float *)b[16], nullptr, stream);
         xla_release(L, s);
     }
     report("rasterize_bwd", rc);

@@ -1,50 +1,74 @@
 // gemm_tc.cu -- BF16 GEMM with FP32 accumulation on the 5th-generation tensor
-// cores (tcgen05), for the warm-start network's convolutions (as implicit
-// im2col GEMMs) and their gradients.
+// cores (tcgen05), for the warm-start network's convolutions (as im2col
+// GEMMs) and their gradients.
 //
 //   C[M,N] (fp32, row-major, ldc) (+)= A[M,K] (bf16, row-major: K-major)
 //                                       x B[N,K]^T (bf16, row-major: K-major)
+//   or, fused into the epilogue, y[M,N] = act(A B^T + bias) as bf16 (or fp32)
 //
-// One CTA of 128 threads computes a 128 x 128 tile of C.  Operand tiles of
-// 128 rows x 64 K-elements are copied into shared memory with cp.async in the
-// tensor cores' no-swizzle K-major layout (8-row x 16-byte core matrices;
-// the next core matrix along K 128 bytes on, along M/N 1024 bytes on), two
-// stages deep.  One thread issues tcgen05.mma (M=128, N=128, K=16, four per
-// stage) into a 128-column FP32 accumulator in tensor memory and commits
-// each stage to an mbarrier; a stage's buffers are refilled only after that
-// barrier flips.  The epilogue reads the accumulator with tcgen05.ld (warp w
-// owns TMEM lanes 32w..32w+31 = tile rows) and writes C.
+// One CTA of 128 threads computes a 128 x BN tile of C (BN = 32, 64 or 128,
+// the smallest that covers N, so narrow layers waste no MMA columns).
+// Operand tiles of 128 (or BN) rows x 64 K-elements arrive by TMA
+// (cp.async.bulk.tensor, tensor maps over this GPU's memory, no multicast)
+// in the 128-byte-swizzled K-major layout the tensor cores read directly,
+// through a ring of kGemmStages stages: thread 0 (producer) waits for a
+// stage's "empty" barrier and issues its two tensor loads onto the stage's
+// "full" barrier; thread 32 (MMA issuer) waits for "full", issues four
+// tcgen05.mma (M 128, N BN, K 16) into a BN-column FP32 accumulator in tensor
+// memory and commits them to the stage's "empty" barrier.  After the last
+// stage a commit to "done" releases the epilogue: every warp reads its 32
+// accumulator lanes (= tile rows) with tcgen05.ld and writes C, or adds the
+// bias, applies the ReLU and writes bf16 -- so the fp32 product is never
+// stored and re-read.
 //
 // Every wait is bounded: a barrier that does not flip within spin_limit
-// polls sets DEV_LOOKBACK_TIMEOUT in the status word, the epilogue is
-// skipped, and the CTA frees its tensor memory and returns.
+// polls sets DEV_LOOKBACK_TIMEOUT in the status word; the CTA then waits (again
+// bounded) for its commits, skips the epilogue, frees its tensor memory and
+// returns.
+#include <cuda.h>  // CUtensorMap and its enums; the encoder comes from the driver entry point
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "splat_internal.cuh"
 
 namespace splat {
 
 constexpr int kGemmBM = 128;
-constexpr int kGemmBN = 128;
-constexpr int kGemmBK = 64;
+constexpr int kGemmBK = 64;  // 64 bf16 = one 128-byte swizzle row
 constexpr int kGemmThreads = 128;
-constexpr int kGemmTileBytes = kGemmBM * kGemmBK * 2;  // 16 KB per operand tile
-constexpr int kGemmSmem = 4 * kGemmTileBytes + 1024;   // 2 stages x (A, B) + alignment slack
-constexpr uint32_t kGemmTmemCols = 128;
+constexpr int kGemmStages = 4;
+constexpr int kGemmATile = kGemmBM * kGemmBK * 2;  // 16 KB
+
+template <int BN>
+constexpr int gemm_stage_bytes() {
+    return kGemmATile + BN * kGemmBK * 2;
+}
+template <int BN>
+constexpr int gemm_smem() {
+    return kGemmStages * gemm_stage_bytes<BN>() + 1024;  // + alignment slack
+}
+
+enum GemmOut { kOutF32 = 0, kOutBiasBF16 = 1, kOutBiasF32 = 2 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Shared-memory matrix descriptor: no swizzle, K-major, leading (K) byte
-// offset 128, stride (M/N) byte offset 1024, descriptor version 1.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzled layout (rows of 128 bytes, 8-row / 1024-byte swizzle atoms, the
+// stage buffers 1024-byte aligned): stride byte offset 1024 between 8-row
+// groups, leading byte offset unused (encoded as 16), descriptor version 1,
+// layout type 2 (128-byte swizzle).  The K-th 16-element slice of a row
+// starts 32 K bytes into it: the hardware applies the swizzle to the
+// address, so advancing the start address selects the slice.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)(128u >> 4) << 16;
+    d |= (uint64_t)1 << 16;
     d |= (uint64_t)(1024u >> 4) << 32;
     d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
     return d;
 }
 
@@ -72,110 +96,163 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_
     return false;
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
-                 "r"(src_bytes)
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n"
+                 ::"r"(bar), "r"(bytes)
                  : "memory");
 }
 
+// 2-D tensor load of the box at (x = K element, y = row) into shared memory,
+// completing on `bar`.  x is a multiple of 64 elements (128 bytes).
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
 struct GemmArgs {
-    const __nv_bfloat16 *A, *B;
-    float *C;
+    float *C;               // kOutF32 / kOutBiasF32 output (ldc)
+    __nv_bfloat16 *y16;     // kOutBiasBF16 output (ldc)
+    const float *bias;      // [N], kOutBias*
     int M, N, K;
-    int lda, ldb, ldc;  // elements
-    int accumulate;     // add to C instead of overwriting
-    int ktiles_per;     // K tiles per CTA along grid z (split K: partial sums added atomically)
+    int ldc;                // elements
+    int accumulate;         // kOutF32: add to C instead of overwriting
+    int relu;               // kOutBias*: max(., 0)
+    int mode;               // GemmOut
+    int ktiles_per;         // K tiles per CTA along grid z (split K: partial sums added atomically)
     uint32_t *status;
     uint32_t spin_limit;
 };
 
-// Copies the 128 x 64 tile at (row0, k0) of a K-major matrix into the
-// core-matrix layout; rows >= rows_total and K past k_total read as zeros.
-__device__ __forceinline__ void load_tile(uint32_t sbase, const __nv_bfloat16 *g, int ld,
-                                          int row0, int rows_total, int k0, int k_total) {
+// Epilogue of one row segment of 16 accumulator columns starting at column n.
+__device__ __forceinline__ void gemm_store16(const GemmArgs &a, int row, int n, const uint32_t r[16],
+                                             bool split) {
+    if (a.mode == kOutF32) {
+        float *crow = a.C + (size_t)row * a.ldc;
 #pragma unroll
-    for (int it = 0; it < (kGemmBM * kGemmBK / 8) / kGemmThreads; ++it) {
-        const int q = it * kGemmThreads + threadIdx.x;  // 16-byte chunk index
-        const int r = q >> 3, c = q & 7;                // row, chunk along K
-        const int row = row0 + r, k = k0 + c * 8;
-        const bool ok = row < rows_total && k < k_total;
-        const __nv_bfloat16 *src = ok ? g + (size_t)row * ld + k : g;
-        const uint32_t dst = sbase + (uint32_t)(((r >> 3) * 8 + c) * 128 + (r & 7) * 16);
-        cp_async16(dst, src, ok ? 16u : 0u);
+        for (int q = 0; q < 16; ++q) {
+            if (n + q >= a.N) break;
+            const float v = __uint_as_float(r[q]);
+            if (split) atomicAdd(&crow[n + q], v);
+            else crow[n + q] = a.accumulate ? crow[n + q] + v : v;
+        }
+        return;
     }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    float v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const int c = min(n + q, a.N - 1);
+        v[q] = __uint_as_float(r[q]) + a.bias[c];
+        if (a.relu) v[q] = fmaxf(v[q], 0.f);
+    }
+    if (a.mode == kOutBiasF32) {
+        float *yrow = a.C + (size_t)row * a.ldc;
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+            if (n + q < a.N) yrow[n + q] = v[q];
+        return;
+    }
+    __nv_bfloat16 *yrow = a.y16 + (size_t)row * a.ldc;
+    if (n + 16 <= a.N && ((reinterpret_cast<uintptr_t>(yrow + n) & 15u) == 0)) {
+        // two 16-byte stores
+        uint4 pk[2];
+        uint32_t *w = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+            w[q] = *reinterpret_cast<const uint32_t *>(&h2);
+        }
+        reinterpret_cast<uint4 *>(yrow + n)[0] = pk[0];
+        reinterpret_cast<uint4 *>(yrow + n)[1] = pk[1];
+    } else {
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+            if (n + q < a.N) yrow[n + q] = __float2bfloat16(v[q]);
+    }
 }
 
-__global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs a) {
+template <int BN>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    gemm_bf16_tc_kernel(const __grid_constant__ CUtensorMap map_a,
+                        const __grid_constant__ CUtensorMap map_b, GemmArgs a) {
+    constexpr uint32_t kStage = (uint32_t)gemm_stage_bytes<BN>();
     extern __shared__ uint8_t g_dyn[];
-    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ __align__(8) uint64_t s_full[kGemmStages];
+    __shared__ __align__(8) uint64_t s_empty[kGemmStages];
+    __shared__ __align__(8) uint64_t s_done;
     __shared__ uint32_t s_tmem;
-    // 1024-byte aligned operand area
-    const uint32_t raw = smem_addr(g_dyn);
-    const uint32_t base = (raw + 1023u) & ~1023u;
-    const uint32_t sA[2] = {base, base + kGemmTileBytes};
-    const uint32_t sB[2] = {base + 2 * kGemmTileBytes, base + 3 * kGemmTileBytes};
+    // 1024-byte aligned stage buffers (the swizzle atoms)
+    const uint32_t base = (smem_addr(g_dyn) + 1023u) & ~1023u;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int m0 = blockIdx.x * kGemmBM, n0 = blockIdx.y * kGemmBN;
-    const uint32_t bar0 = smem_addr(&s_bar[0]), bar1 = smem_addr(&s_bar[1]);
+    const int m0 = blockIdx.x * kGemmBM, n0 = blockIdx.y * BN;
+    const uint32_t done_bar = smem_addr(&s_done);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                          smem_addr(&s_tmem)),
-                     "r"(kGemmTmemCols)
+                     "r"((uint32_t)BN)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar1) : "memory");
-        // make the initialised barriers visible to the tensor cores' arrivals
+        for (int s = 0; s < kGemmStages; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_full[s]))
+                         : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_empty[s]))
+                         : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(done_bar) : "memory");
+        // make the initialised barriers visible to the async proxy (TMA,
+        // tensor-core commits)
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = s_tmem;
-    const uint32_t idesc = mma_idesc(kGemmBM, kGemmBN);
     const int kt0 = blockIdx.z * a.ktiles_per;
     const int ktiles = max(0, min(a.ktiles_per, (a.K + kGemmBK - 1) / kGemmBK - kt0));
     const bool split = gridDim.z > 1;
 
-    if (ktiles > 0) {
-        load_tile(sA[0], a.A, a.lda, m0, a.M, kt0 * kGemmBK, a.K);
-        load_tile(sB[0], a.B, a.ldb, n0, a.N, kt0 * kGemmBK, a.K);
-    }
     bool ok = true;
-    for (int kt = 0; kt < ktiles; ++kt) {
-        const int st = kt & 1;
-        if (kt + 1 < ktiles) {
-            if (kt >= 1) {  // the MMAs of tile kt-1 read the buffers about to be refilled
-                const int j = kt - 1;
-                const bool done = mbar_wait((j & 1) ? bar1 : bar0, (uint32_t)((j >> 1) & 1),
-                                            a.spin_limit);
-                if (!__syncthreads_and(done)) {  // a block-uniform decision
-                    ok = false;
-                    break;
-                }
+    if (ktiles > 0 && t == 0) {  // producer: TMA loads into the ring
+        for (int kt = 0; kt < ktiles; ++kt) {
+            const int s = kt % kGemmStages;
+            if (kt >= kGemmStages &&
+                !mbar_wait(smem_addr(&s_empty[s]), (uint32_t)((kt / kGemmStages - 1) & 1),
+                           a.spin_limit)) {
+                ok = false;
+                break;
             }
-            load_tile(sA[st ^ 1], a.A, a.lda, m0, a.M, (kt0 + kt + 1) * kGemmBK, a.K);
-            load_tile(sB[st ^ 1], a.B, a.ldb, n0, a.N, (kt0 + kt + 1) * kGemmBK, a.K);
-            asm volatile("cp.async.wait_group 2;\n" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            const uint32_t full = smem_addr(&s_full[s]);
+            const uint32_t sa = base + (uint32_t)s * kStage;
+            mbar_arrive_tx(full, kStage);
+            const int x = (kt0 + kt) * kGemmBK;
+            tma_load_2d(sa, &map_a, x, m0, full);
+            tma_load_2d(sa + (uint32_t)kGemmATile, &map_b, x, n0, full);
         }
-        // the copies were made through the generic proxy; the tensor cores
-        // read through the async proxy
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
-        if (t == 0) {
+    } else if (ktiles > 0 && t == 32) {  // MMA issuer
+        const uint32_t idesc = mma_idesc(kGemmBM, BN);
+        for (int kt = 0; kt < ktiles; ++kt) {
+            const int s = kt % kGemmStages;
+            if (!mbar_wait(smem_addr(&s_full[s]), (uint32_t)((kt / kGemmStages) & 1),
+                           a.spin_limit)) {
+                ok = false;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sa = base + (uint32_t)s * kStage, sb = sa + (uint32_t)kGemmATile;
 #pragma unroll
-            for (int s = 0; s < kGemmBK / 16; ++s) {
-                const uint64_t ad = smem_desc(sA[st] + (uint32_t)s * 256u);
-                const uint64_t bd = smem_desc(sB[st] + (uint32_t)s * 256u);
-                const uint32_t acc = (kt > 0 || s > 0) ? 1u : 0u;
+            for (int ks = 0; ks < kGemmBK / 16; ++ks) {
+                const uint64_t ad = smem_desc_sw128(sa + (uint32_t)ks * 32u);
+                const uint64_t bd = smem_desc_sw128(sb + (uint32_t)ks * 32u);
+                const uint32_t acc = (kt > 0 || ks > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
@@ -183,27 +260,32 @@ __global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs 
                     "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
                     : "memory");
             }
+            // frees the stage once these MMAs have read it
             asm volatile(
                 "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                    st ? bar1 : bar0)
+                    smem_addr(&s_empty[s]))
                 : "memory");
         }
+        if (ok)
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                    done_bar)
+                : "memory");
     }
-    if (ok && ktiles > 0) {
-        const int j = ktiles - 1;
-        ok = mbar_wait((j & 1) ? bar1 : bar0, (uint32_t)((j >> 1) & 1), a.spin_limit);
-    }
+    __syncwarp();
+    if (ktiles > 0) ok = mbar_wait(done_bar, 0u, a.spin_limit) && ok;
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (!ok) {
         if (t == 0) raise_status(a.status, DEV_LOOKBACK_TIMEOUT);
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        // let whatever was issued finish before the CTA's memory goes away
+        mbar_wait(done_bar, 0u, a.spin_limit);
     } else if (ktiles > 0) {
         const int row = m0 + warp * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
-        for (int c = 0; c < kGemmBN; c += 16) {
+        for (int c = 0; c < BN; c += 16) {
             uint32_t r[16];
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -214,18 +296,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs 
                 : "r"(lane_addr + (uint32_t)c)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (row < a.M) {
-                float *crow = a.C + (size_t)row * a.ldc;
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int n = n0 + c + q;
-                    if (n < a.N) {
-                        const float v = __uint_as_float(r[q]);
-                        if (split) atomicAdd(&crow[n], v);
-                        else crow[n] = a.accumulate ? crow[n] + v : v;
-                    }
-                }
-            }
+            if (row < a.M && n0 + c < a.N) gemm_store16(a, row, n0 + c, r, split);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -233,9 +304,95 @@ __global__ void __launch_bounds__(kGemmThreads, 1) gemm_bf16_tc_kernel(GemmArgs 
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
-                     "r"(kGemmTmemCols)
+                     "r"((uint32_t)BN)
                      : "memory");
     }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// Tensor map of a row-major bf16 matrix (rows x k, ld elements per row) read
+// in boxes of 64 K-elements x box_rows rows, 128-byte swizzle, zeros outside.
+static int make_operand_map(CUtensorMap *map, const void *ptr, int rows, int k, int ld,
+                            int box_rows) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return fail(SPLAT_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2u};
+    const cuuint32_t box[2] = {(cuuint32_t)kGemmBK, (cuuint32_t)box_rows};
+    const cuuint32_t elem[2] = {1u, 1u};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims,
+                          strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SPLAT_ERR_INVALID_ARG, "tensor map encode failed (%d)", (int)r);
+    return SPLAT_OK;
+}
+
+template <int BN>
+static int launch_gemm(const void *A, const void *B, GemmArgs g, int lda, int ldb,
+                       cudaStream_t stream) {
+    alignas(64) CUtensorMap ma, mb;
+    if (int rc = make_operand_map(&ma, A, g.M, g.K, lda, kGemmBM)) return rc;
+    if (int rc = make_operand_map(&mb, B, g.N, g.K, ldb, BN)) return rc;
+    auto kernel = gemm_bf16_tc_kernel<BN>;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             gemm_smem<BN>()) != cudaSuccess)
+        return check_launch("gemm shared-memory attribute");
+    const int gm = (g.M + kGemmBM - 1) / kGemmBM, gn = (g.N + BN - 1) / BN;
+    const int kt_total = (g.K + kGemmBK - 1) / kGemmBK;
+    // split K (kOutF32 only) when the output has few tiles and K is long:
+    // partial sums of `ktiles_per` K tiles each are added atomically into C
+    // (zeroed first unless accumulating)
+    int splits = 1;
+    if (g.mode == kOutF32 && gm * gn < 152 && kt_total >= 16)
+        splits = std::min(std::max(1, 2 * 152 / (gm * gn)), kt_total / 8);
+    g.ktiles_per = std::max(1, (kt_total + splits - 1) / splits);
+    splits = std::max(1, (kt_total + g.ktiles_per - 1) / g.ktiles_per);
+    if (splits > 1 && !g.accumulate &&
+        cudaMemset2DAsync(g.C, sizeof(float) * (size_t)g.ldc, 0, sizeof(float) * (size_t)g.N,
+                          (size_t)g.M, stream) != cudaSuccess)
+        return check_launch("gemm split-K zero");
+    dim3 grid(gm, gn, splits);
+    kernel<<<grid, kGemmThreads, gemm_smem<BN>(), stream>>>(ma, mb, g);
+    return check_launch("gemm_bf16_tc_kernel");
+}
+
+static int check_operands(const void *A, const void *B, int M, int N, int K, int lda, int ldb) {
+    if (M < 0 || N < 0 || K < 0) return fail(SPLAT_ERR_INVALID_ARG, "negative GEMM size");
+    if (!A || !B) return fail(SPLAT_ERR_INVALID_ARG, "GEMM operand is NULL");
+    if (K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K)
+        return fail(SPLAT_ERR_INVALID_ARG,
+                    "GEMM needs K, lda, ldb multiples of 8 (16-byte rows), lda, ldb >= K");
+    if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16)
+        return fail(SPLAT_ERR_INVALID_ARG, "GEMM operands must be 16-byte aligned");
+    return SPLAT_OK;
+}
+
+static int run_gemm(const void *A, const void *B, GemmArgs g, int lda, int ldb,
+                    cudaStream_t stream) {
+    if (g.N <= 32) return launch_gemm<32>(A, B, g, lda, ldb, stream);
+    if (g.N <= 64) return launch_gemm<64>(A, B, g, lda, ldb, stream);
+    return launch_gemm<128>(A, B, g, lda, ldb, stream);
 }
 
 }  // namespace splat
@@ -248,38 +405,8 @@ int splat_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
                     int ldc, int accumulate, uint32_t *status_dev, splat_stream_t stream) {
     if (M < 0 || N < 0 || K < 0) return fail(SPLAT_ERR_INVALID_ARG, "negative GEMM size");
     if (M == 0 || N == 0) return SPLAT_OK;
-    if (!A || !B || !C) return fail(SPLAT_ERR_INVALID_ARG, "GEMM operand is NULL");
-    if (K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N)
-        return fail(SPLAT_ERR_INVALID_ARG,
-                    "GEMM needs K, lda, ldb multiples of 8 (16-byte rows), lda, ldb >= K, ldc >= N");
-    if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16)
-        return fail(SPLAT_ERR_INVALID_ARG, "GEMM operands must be 16-byte aligned");
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(gemm_bf16_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 kGemmSmem) != cudaSuccess)
-            return check_launch("gemm shared-memory attribute");
-        attr_set = true;
-    }
-    GemmArgs g;
-    g.A = static_cast<const __nv_bfloat16 *>(A);
-    g.B = static_cast<const __nv_bfloat16 *>(B);
-    g.C = C;
-    g.M = M; g.N = N; g.K = K;
-    g.lda = lda; g.ldb = ldb; g.ldc = ldc;
-    g.accumulate = accumulate;
-    g.status = status_dev;
-    g.spin_limit = 1u << 21;  // ~0.2 s of polling per wait
-    // split K when the output has few tiles and K is long: partial sums of
-    // `ktiles_per` K tiles each are added atomically into C (zeroed first
-    // unless accumulating)
-    const int gm = (M + kGemmBM - 1) / kGemmBM, gn = (N + kGemmBN - 1) / kGemmBN;
-    const int kt_total = (K + kGemmBK - 1) / kGemmBK;
-    int splits = 1;
-    if (gm * gn < 152 && kt_total >= 16)
-        splits = std::min(std::max(1, 2 * 152 / (gm * gn)), kt_total / 8);
-    g.ktiles_per = std::max(1, (kt_total + splits - 1) / splits);
-    splits = std::max(1, (kt_total + g.ktiles_per - 1) / g.ktiles_per);
+    if (int rc = check_operands(A, B, M, N, K, lda, ldb)) return rc;
+    if (!C || ldc < N) return fail(SPLAT_ERR_INVALID_ARG, "GEMM needs C and ldc >= N");
     if (K == 0) {
         if (accumulate) return SPLAT_OK;
         if (cudaMemset2DAsync(C, sizeof(float) * (size_t)ldc, 0, sizeof(float) * (size_t)N,
@@ -287,13 +414,37 @@ int splat_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K,
             return check_launch("gemm zero");
         return SPLAT_OK;
     }
-    if (splits > 1 && !accumulate &&
-        cudaMemset2DAsync(C, sizeof(float) * (size_t)ldc, 0, sizeof(float) * (size_t)N, (size_t)M,
-                          (cudaStream_t)stream) != cudaSuccess)
-        return check_launch("gemm split-K zero");
-    dim3 grid(gm, gn, splits);
-    gemm_bf16_tc_kernel<<<grid, kGemmThreads, kGemmSmem, (cudaStream_t)stream>>>(g);
-    return check_launch("gemm_bf16_tc_kernel");
+    GemmArgs g{};
+    g.C = C;
+    g.M = M; g.N = N; g.K = K;
+    g.ldc = ldc;
+    g.accumulate = accumulate;
+    g.mode = kOutF32;
+    g.status = status_dev;
+    g.spin_limit = 1u << 21;  // ~0.2 s of polling per wait
+    return run_gemm(A, B, g, lda, ldb, (cudaStream_t)stream);
+}
+
+int splat_gemm_bf16_bias_act(const void *A, const void *B, const float *bias, void *y16,
+                             float *y32, int M, int N, int K, int lda, int ldb, int ldy, int relu,
+                             uint32_t *status_dev, splat_stream_t stream) {
+    if (M < 0 || N < 0 || K < 0) return fail(SPLAT_ERR_INVALID_ARG, "negative GEMM size");
+    if (M == 0 || N == 0) return SPLAT_OK;
+    if (int rc = check_operands(A, B, M, N, K, lda, ldb)) return rc;
+    if (!bias || (!y16 == !y32) || ldy < N || K == 0)
+        return fail(SPLAT_ERR_INVALID_ARG,
+                    "GEMM + bias needs K > 0, a bias, exactly one of y16 / y32 and ldy >= N");
+    GemmArgs g{};
+    g.C = y32;
+    g.y16 = static_cast<__nv_bfloat16 *>(y16);
+    g.bias = bias;
+    g.M = M; g.N = N; g.K = K;
+    g.ldc = ldy;
+    g.relu = relu;
+    g.mode = y16 ? kOutBiasBF16 : kOutBiasF32;
+    g.status = status_dev;
+    g.spin_limit = 1u << 21;
+    return run_gemm(A, B, g, lda, ldb, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -193,9 +193,10 @@ struct RasterFwdArgs {
     float *v_img, *loss;
     float inv_count;
     // Optional (16x16 tiles): one byte per sorted-list slot, bit w set when
-    // some pixel of warp w blended that entry; the backward walks exactly
-    // those entries.  Written for every entry of each batch the tile
-    // processes (all entries up to the tile's largest final_idx).
+    // some pixel of warp w passed that entry's alpha test (it blended the
+    // entry, or saturated at it); the backward walks only those entries.
+    // Written for every entry of each batch the tile processes (all entries
+    // up to the tile's largest final_idx).
     uint8_t *blend;
 };
 
@@ -414,7 +415,7 @@ constexpr int kF16Threads = 128;
 constexpr int kF16Warps = 4;
 constexpr int kF16Batch = 256;
 
-// The warps that blended each entry of a batch: byte w of word e is set by
+// The warps that passed each entry of a batch: byte w of word e is set by
 // warp w (plain byte stores, one warp per byte), then packed to bits 0-3.
 __device__ __forceinline__ uint8_t pack_blend_bytes(uint32_t x) {
     x &= 0x01010101u;
@@ -523,10 +524,10 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
             const bool stop0 = pass0 && next_T.x <= 1e-4f;
             const bool stop1 = pass1 && next_T.y <= 1e-4f;
             const bool bl0 = pass0 && !stop0, bl1 = pass1 && !stop1;
-            if (kBlend) {
-                const unsigned blended = __ballot_sync(0xffffffffu, bl0 || bl1);
-                if (lane == 0 && blended) reinterpret_cast<uint8_t *>(s_blend)[4 * t + warp] = 1;
-            }
+            // some pixel of this warp passed the entry's test: it blended
+            // the entry, or stopped at it (the one entry past its final_idx
+            // that the backward then walks for nothing)
+            if (kBlend && lane == 0) reinterpret_cast<uint8_t *>(s_blend)[4 * t + warp] = 1;
             const float2 vis = mul2(make_float2(bl0 ? al0 : 0.f, bl1 ? al1 : 0.f), T);
             acc_r = fma2(f2(r1.z), vis, acc_r);
             acc_g = fma2(f2(r1.w), vis, acc_g);
@@ -905,7 +906,7 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
             const int idx = batch_end - e;
             if (idx >= range.x) {
                 // with the forward's blend bytes, an entry that no warp
-                // blended is never gathered
+                // passed is never gathered, and the bytes replace the box test
                 const unsigned bm = kBlend ? (unsigned)a.blend[idx] : 0u;
                 if (kBlend && bm == 0u) {
                     s_mask[e] = 0u;

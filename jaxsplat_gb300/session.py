@@ -121,6 +121,8 @@ class RenderSession(StreamingSteps):
     def _size(self, capacity: int):
         self.capacity = max(int(capacity), 1)
         self.ids_sorted = torch.empty(self.capacity, dtype=torch.int32, device=self.dev)
+        # the forward's per-slot warp bytes for the backward (block width 16)
+        self.blend = torch.empty(self.capacity, dtype=torch.uint8, device=self.dev)
         nbytes = self.lib.splat_sort_workspace_size(C.byref(self.params), self.capacity)
         self.sort_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.dev)
         self.graph = None
@@ -206,13 +208,13 @@ class RenderSession(StreamingSteps):
         self._check(lib.splat_rasterize_fwd_l2(
             pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),
             P(self.background), P(self.target), P(self.final_Ts), P(self.final_idx),
-            P(self.img), P(self.v_img), P(self.loss), s), "rasterize_fwd_l2")
+            P(self.img), P(self.v_img), P(self.loss), P(self.blend), s), "rasterize_fwd_l2")
         mark("raster_bwd")
         self._check(lib.splat_rasterize_bwd(
             pr, cap, P(self.total), P(self.ids_sorted), P(self.tile_bins), P(self.packed),
             P(self.background), P(self.final_Ts), P(self.final_idx), P(self.v_img),
             P(self.v_alpha), P(self.v_colors), P(self.v_opacity), P(self.v_xy), None,
-            P(self.v_conic), s), "rasterize_bwd")
+            P(self.v_conic), P(self.blend), s), "rasterize_bwd")
         mark("project_bwd")
         self._check(lib.splat_project_bwd(
             pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat), P(self.cov3d),

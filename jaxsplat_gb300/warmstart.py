@@ -6,8 +6,9 @@ convolutions 3->32->64->128->256 (ReLU, BF16 activations and weights, FP32
 accumulation) down to a 32x32 grid, and a 1x1 convolution head emitting, per
 grid cell, 16 Gaussians x 14 raw parameters.  Every convolution runs as
 im2col + the tcgen05 BF16 GEMM of this library (gemm_tc.cu), forward and
-backward; the surrounding gathers, bias/ReLU and Adam are this library's
-kernels too (nn.cu).  torch only holds the buffers.
+backward; in the forward the bias, ReLU and bf16 conversion run in the
+GEMM's epilogue.  The surrounding gathers, ReLU gradient and Adam are this
+library's kernels too (nn.cu).  torch only holds the buffers.
 
 Training data is what the plain fitting loop itself produces (``Fitter``
 from random init on procedural targets): each fitted set is put on the grid
@@ -87,6 +88,16 @@ class ConvNet:
         _lib.check(self.lib.splat_gemm_bf16(_p(A), _p(B), _p(Cm), M, N, K, lda, ldb, ldc, int(acc),
                                             _p(self.status), self._s()), "gemm_bf16")
 
+    def gemm_bias_act(self, A, B, bias, M, N, K, relu, bf16_out=True):
+        """act(A B^T + bias) with the bias, ReLU and output conversion fused
+        into the GEMM's epilogue: (M, N) bf16 (or fp32)."""
+        y = torch.empty(M, N, dtype=torch.bfloat16 if bf16_out else torch.float32,
+                        device=self.dev)
+        _lib.check(self.lib.splat_gemm_bf16_bias_act(
+            _p(A), _p(B), _p(bias), _p(y) if bf16_out else None, None if bf16_out else _p(y),
+            M, N, K, K, K, N, int(relu), _p(self.status), self._s()), "gemm_bf16_bias_act")
+        return y
+
     def transpose(self, x, rows, cols):
         out = torch.empty(cols, rows, dtype=torch.bfloat16, device=self.dev)
         _lib.check(self.lib.splat_nn_transpose_bf16(_p(x), _p(out), rows, cols, rows, self._s()),
@@ -107,20 +118,13 @@ class ConvNet:
             cols = torch.empty(P, L["k"], dtype=torch.bfloat16, device=self.dev)
             _lib.check(lib.splat_nn_im2col3x3(_p(cur), _p(cols), B, h, h, L["cin"], 2, L["k"], s),
                        "im2col3x3")
-            acc = torch.empty(P, L["cout"], device=self.dev)
-            self.gemm(cols, L["w16"], acc, P, L["cout"], L["k"], L["k"], L["k"], L["cout"])
-            y = torch.empty(P, L["cout"], dtype=torch.bfloat16, device=self.dev)
-            _lib.check(lib.splat_nn_bias_act(_p(acc), _p(L["b"]), _p(y), None, P, L["cout"], 1, s),
-                       "bias_act")
+            y = self.gemm_bias_act(cols, L["w16"], L["b"], P, L["cout"], L["k"], relu=True)
             self.saved.append((cols, y, h, ho, P))
             cur, h = y, ho
         Hd = self.head
         P = cur.shape[0]
-        acc = torch.empty(P, Hd["cout"], device=self.dev)
-        self.gemm(cur, Hd["w16"], acc, P, Hd["cout"], Hd["k"], Hd["k"], Hd["k"], Hd["cout"])
-        out = torch.empty(P, Hd["cout"], device=self.dev)
-        _lib.check(lib.splat_nn_bias_act(_p(acc), _p(Hd["b"]), None, _p(out), P, Hd["cout"], 0, s),
-                   "bias_act")
+        out = self.gemm_bias_act(cur, Hd["w16"], Hd["b"], P, Hd["cout"], Hd["k"], relu=False,
+                                 bf16_out=False)
         self.head_in = cur
         self.batch = B
         return out
@@ -310,6 +314,14 @@ class WarmStart:
         grid = out.cpu().numpy() * self.sd + self.mu
         return from_grid(grid)
 
+    def propose_mean(self, image=None) -> dict:
+        """The ablation of ``propose``: the network's output forced to zero,
+        i.e. the training sets' mean slot parameters in every cell of the
+        grid -- the same grid layout and dataset statistics, nothing taken
+        from the target image."""
+        grid = np.tile(self.mu, (GRID * GRID, 1))
+        return from_grid(grid)
+
 
 def time_to_psnr(fitter: Fitter, target, seed: int = 0, psnr: float = 30.0,
                  max_steps: int = 3000, check_every: int = 5, propose=None):
@@ -361,7 +373,10 @@ def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
                    eval_seeds=tuple(range(1_000_000, 1_000_008)), psnr: float = 30.0,
                    check_every: int = 5, device="cuda", log=None) -> dict:
     """Dataset from the plain loop, training, then wall-clock to `psnr` dB on
-    held-out seeds from random init and from the network's proposal."""
+    held-out seeds from three starts: random init (the plain method), the
+    network's proposal, and the ablation that keeps the proposal's grid
+    layout and dataset-mean slot parameters but ignores the image
+    (``WarmStart.propose_mean``)."""
     from .scenes import procedural_target
 
     t0 = time.perf_counter()
@@ -378,17 +393,25 @@ def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
     # untimed warm-up of both paths (first-use costs)
     time_to_psnr(ft, first, psnr=psnr, max_steps=20, check_every=check_every)
     time_to_psnr(ft, first, psnr=psnr, max_steps=20, check_every=check_every, propose=ws.propose)
+    time_to_psnr(ft, first, psnr=psnr, max_steps=20, check_every=check_every,
+                 propose=ws.propose_mean)
     for sd in eval_seeds:
         tgt = procedural_target(sd, IMG, device=device).cpu().numpy()
         plain = time_to_psnr(ft, tgt, seed=sd, psnr=psnr, check_every=check_every)
         learned = time_to_psnr(ft, tgt, seed=sd, psnr=psnr, check_every=check_every,
                                propose=ws.propose)
+        mean = time_to_psnr(ft, tgt, seed=sd, psnr=psnr, check_every=check_every,
+                            propose=ws.propose_mean)
         ft.reset(tgt, init=ws.propose(tgt))
         init_psnr = ft.check_render()
+        ft.reset(tgt, init=ws.propose_mean(tgt))
+        mean_init_psnr = ft.check_render()
         rows.append({"seed": int(sd), "plain_s": round(plain[2], 4), "plain_steps": plain[1],
                      "plain_reached": bool(plain[0]), "learned_s": round(learned[2], 4),
                      "learned_steps": learned[1], "learned_reached": bool(learned[0]),
-                     "learned_init_psnr": round(init_psnr, 2)})
+                     "learned_init_psnr": round(init_psnr, 2), "mean_s": round(mean[2], 4),
+                     "mean_steps": mean[1], "mean_reached": bool(mean[0]),
+                     "mean_init_psnr": round(mean_init_psnr, 2)})
         if log:
             log(str(rows[-1]))
     return {"train_sets": n_train, "fit_steps": fit_steps, "epochs": epochs,

@@ -15,10 +15,12 @@ def to_dev(inp: dict) -> dict:
             for k in INPUT_KEYS if k in inp}
 
 
-def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True, device=False) -> dict:
+def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True, device=False,
+             blend=True) -> dict:
     """project -> sort/bin (with intermediates) -> rasterize fwd [-> bwd chain].
     Returns numpy arrays, or the CUDA tensors themselves with ``device``;
-    ``v_img`` may be a numpy array or a CUDA tensor."""
+    ``v_img`` may be a numpy array or a CUDA tensor.  With ``blend`` (block
+    width 16) the backward walks the forward's per-slot warp bytes."""
     t = to_dev(inp)
     p = _ops.project_fwd(t["means3d"], t["scales"], t["quats"], t["viewmat"], block_width=bw,
                          **kw)
@@ -29,7 +31,9 @@ def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True, device=Fal
     packed = _ops.pack_splats(p["xys"], p["conics"], t["colors"], t["opacities"],
                               img_shape=kw["img_shape"], block_width=bw)
     r = _ops.rasterize_fwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed,
-                           t["background"], img_shape=kw["img_shape"], block_width=bw)
+                           t["background"], img_shape=kw["img_shape"], block_width=bw,
+                           blend=blend)
+    blend_bytes = r.pop("blend", None)
     out = {**p, **s, **r}
     out.pop("total")
     out["count"] = torch.tensor(count)
@@ -40,7 +44,7 @@ def run_cuda(inp: dict, kw: dict, bw: int, v_img=None, with_abs=True, device=Fal
         rb = _ops.rasterize_bwd(count, s["gaussian_ids_sorted"], s["tile_bins"], packed,
                                 t["background"], r["final_Ts"], r["final_idx"], vi,
                                 torch.zeros(h, w, 1, device="cuda"), img_shape=kw["img_shape"],
-                                block_width=bw, with_abs=with_abs)
+                                block_width=bw, with_abs=with_abs, blend=blend_bytes)
         z = torch.zeros(n, 1, device="cuda")
         pb = _ops.project_bwd(t["means3d"], t["scales"], t["quats"], t["viewmat"], p["cov3d"],
                               p["radii"], p["conics"], p["compensation"], rb["v_xy"], z,

@@ -158,7 +158,7 @@ def test_invalid_sizes_rejected_without_gpu(lib, n, shape, bw, msg):
 
     p = _lib.make_params(n, shape, block_width=bw)
     for call in (lambda: lib.splat_project_fwd(C.byref(p), *([None] * 13), None, 0, None),
-                 lambda: lib.splat_rasterize_fwd(C.byref(p), 0, *([None] * 8), None),
+                 lambda: lib.splat_rasterize_fwd(C.byref(p), 0, *([None] * 9), None),
                  lambda: lib.splat_project_bwd(C.byref(p), *([None] * 17), None)):
         assert call() == 1
         assert msg in lib.splat_last_error()
@@ -193,7 +193,7 @@ def test_misaligned_tile_bins_rejected_without_gpu(lib):
     p = _lib.make_params(10, (32, 32), (32.0, 32.0), (16.0, 16.0), 1.0, 0.01, 16)
     fake = [C.c_void_p(0x10000 + 256 * i) for i in range(8)]
     rc = lib.splat_rasterize_fwd(C.byref(p), 100, None, fake[0], C.c_void_p(0x30004), fake[1],
-                                 fake[2], fake[3], fake[4], fake[5], None)
+                                 fake[2], fake[3], fake[4], fake[5], None, None)
     assert rc == 1 and b"8-byte aligned" in lib.splat_last_error()
 
 

@@ -1,6 +1,8 @@
-"""The tcgen05 BF16 GEMM (splat_gemm_bf16) against an fp32 product of the
-same bf16 operands: full and partial tiles, K not a multiple of the K tile,
-strided operands, accumulation."""
+"""The tcgen05 BF16 GEMM (splat_gemm_bf16, TMA-fed) against an fp32 product of
+the same bf16 operands: full and partial tiles, narrow N (the 32- and
+64-column tiles), K not a multiple of the K tile, strided operands,
+accumulation, split K; and its fused bias + ReLU epilogue
+(splat_gemm_bf16_bias_act) to bf16 and fp32."""
 
 import ctypes as C
 
@@ -30,7 +32,8 @@ def _gemm(A, B, Cm, accumulate=False, lda=None, ldb=None):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 384, 192), (300, 200, 72),
-                                   (1000, 32, 8), (77, 256, 1152)])
+                                   (1000, 32, 8), (77, 256, 1152), (520, 64, 288),
+                                   (4100, 48, 40), (64, 288, 2048)])
 def test_gemm_matches_fp32_product(M, N, K):
     import torch
 
@@ -56,3 +59,39 @@ def test_gemm_strided_and_accumulate():
     _gemm(A, B, Cm, accumulate=True)
     ref = C0 + A.float() @ B.float().T
     assert (Cm - ref).abs().max().item() <= 1e-3
+
+
+@pytest.mark.parametrize("M,N,K,relu,bf16", [(1000, 32, 32, True, True), (333, 64, 288, True, True),
+                                             (257, 128, 576, True, True),
+                                             (300, 224, 256, False, False)])
+def test_gemm_bias_act_epilogue(M, N, K, relu, bf16):
+    import torch
+
+    from jaxsplat_gb300 import _lib
+    from jaxsplat_gb300._ops import _status_word
+
+    lib = _lib.load()
+    g = torch.Generator(device="cuda").manual_seed(M + N + K)
+    A = torch.randn(M, K, device="cuda", generator=g).bfloat16()
+    B = torch.randn(N, K, device="cuda", generator=g).bfloat16()
+    bias = torch.randn(N, device="cuda", generator=g)
+    y = torch.full((M, N), float("nan"), device="cuda",
+                   dtype=torch.bfloat16 if bf16 else torch.float32)
+    st = _status_word(A.device)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    rc = lib.splat_gemm_bf16_bias_act(p(A), p(B), p(bias), p(y) if bf16 else None,
+                                      None if bf16 else p(y), M, N, K, K, K, N, int(relu), p(st),
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "gemm_bf16_bias_act")
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    ref = A.float() @ B.float().T + bias
+    if relu:
+        ref = ref.clamp_min(0)
+    if bf16:
+        # the fp32 sum rounded once to bf16: within one bf16 ulp of the
+        # rounded reference
+        err = (y.float() - ref.bfloat16().float()).abs()
+        assert bool((err <= ref.abs() * 2 ** -7 + 1e-3 * max(1.0, K / 64)).all())
+    else:
+        assert (y - ref).abs().max().item() <= 1e-4 * max(1.0, ref.abs().max().item()) * max(1.0, K / 64)

@@ -1,6 +1,8 @@
 """The warm-start network's convolutions (im2col + tcgen05 GEMM, bias/ReLU,
-col2im) against torch's fp32 conv2d on the same bf16-rounded operands,
-forward and backward, and a short training run that lowers the loss."""
+col2im): one layer's forward and gradients against an fp64 CPU computation on
+the same bf16 operands, the whole network against torch's fp32 conv2d, a
+short training run that lowers the loss, and the learned warm start's gain
+over plain fitting and over its image-blind ablation."""
 
 import numpy as np
 import pytest
@@ -47,6 +49,104 @@ def test_conv_layer_forward_backward_match_torch():
         gw = L["gw"][:, :9 * L["cin"]].reshape(L["cout"], 3, 3, L["cin"]).permute(0, 3, 1, 2)
         assert _rel(gw, w.grad) < 5e-2, L["cin"]
         assert _rel(L["gb"], b.grad) < 5e-2, L["cin"]
+
+
+def _bf16(a):
+    """Round to bfloat16 (nearest, ties to even), returned as float64."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _im2col(x, stride=2):
+    """(n, h, w, c) -> (n*ho*wo, 9c), column (ky*3 + kx)*c + ch, zero padding 1."""
+    n, h, w, c = x.shape
+    ho, wo = (h - 1) // stride + 1, (w - 1) // stride + 1
+    xp = np.pad(x, ((0, 0), (1, 1), (1, 1), (0, 0)))
+    cols = np.empty((n, ho, wo, 3, 3, c))
+    for ky in range(3):
+        for kx in range(3):
+            cols[:, :, :, ky, kx] = xp[:, ky:ky + stride * ho:stride, kx:kx + stride * wo:stride]
+    return cols.reshape(n * ho * wo, 9 * c)
+
+
+def _col2im(dcols, shape, stride=2):
+    """The adjoint of _im2col."""
+    n, h, w, c = shape
+    ho, wo = (h - 1) // stride + 1, (w - 1) // stride + 1
+    d = dcols.reshape(n, ho, wo, 3, 3, c)
+    dxp = np.zeros((n, h + 2, w + 2, c))
+    for ky in range(3):
+        for kx in range(3):
+            dxp[:, ky:ky + stride * ho:stride, kx:kx + stride * wo:stride] += d[:, :, :, ky, kx]
+    return dxp[:, 1:-1, 1:-1]
+
+
+def test_conv_layer_matches_fp64_cpu():
+    """Layer 2 of the encoder (32 -> 64 channels, 3x3 stride 2) on the GPU --
+    im2col, tcgen05 GEMM, bias + ReLU, and in the backward the ReLU mask,
+    bias sums, weight-gradient GEMM, data-gradient GEMM and col2im -- against
+    the same operations in fp64 numpy on the same bf16 operands.  The gathers
+    and the bf16 roundings match exactly; the fp32-accumulated GEMMs within
+    1e-5 normwise of the fp64 products (each is printed)."""
+    import ctypes as C
+
+    import torch
+
+    from jaxsplat_gb300 import _lib
+    from jaxsplat_gb300.warmstart import ConvNet
+
+    net = ConvNet("cuda", seed=3)
+    lib = net.lib
+    L = net.layers[1]
+    n, h, cin, cout, kp = 2, 32, L["cin"], L["cout"], L["k"]
+    ho = (h - 1) // 2 + 1
+    P = n * ho * ho
+    rng = np.random.default_rng(7)
+    x = torch.from_numpy(rng.normal(size=(n, h, h, cin)).astype(np.float32)).cuda().bfloat16()
+    L["b"].copy_(torch.from_numpy(rng.normal(scale=0.1, size=cout).astype(np.float32)))
+    s = net._s()
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    cols = torch.empty(P, kp, dtype=torch.bfloat16, device="cuda")
+    _lib.check(lib.splat_nn_im2col3x3(p(x), p(cols), n, h, h, cin, 2, kp, s), "im2col")
+    acc = torch.empty(P, cout, device="cuda")
+    net.gemm(cols, L["w16"], acc, P, cout, kp, kp, kp, cout)
+    y = torch.empty(P, cout, dtype=torch.bfloat16, device="cuda")
+    _lib.check(lib.splat_nn_bias_act(p(acc), p(L["b"]), p(y), None, P, cout, 1, s), "bias_act")
+    dy = torch.from_numpy(rng.normal(size=(P, cout)).astype(np.float32)).cuda()
+    dz = torch.empty(P, cout, dtype=torch.bfloat16, device="cuda")
+    gb = torch.zeros(cout, device="cuda")
+    _lib.check(lib.splat_nn_act_grad(p(dy), p(y), p(dz), p(gb), P, cout, 1, s), "act_grad")
+    gw = torch.empty(cout, kp, device="cuda")
+    net.gemm(net.transpose(dz, P, cout), net.transpose(cols, P, kp), gw, cout, kp, P, P, P, kp)
+    dcols = torch.empty(P, kp, device="cuda")
+    net.gemm(dz, net.transpose(L["w16"], cout, kp), dcols, P, kp, cout, cout, cout, kp)
+    dx = torch.empty(n, h, h, cin, device="cuda")
+    _lib.check(lib.splat_nn_col2im3x3(p(dcols), p(dx), n, h, h, cin, 2, kp, s), "col2im")
+    torch.cuda.synchronize()
+    f64 = lambda t: t.float().cpu().numpy().astype(np.float64)  # noqa: E731
+
+    x64, W = f64(x), f64(L["w16"])[:, :9 * cin]
+    cols_ref = _im2col(x64)
+    np.testing.assert_array_equal(f64(cols)[:, :9 * cin], cols_ref)
+    assert not f64(cols)[:, 9 * cin:].any()
+    z = cols_ref @ W.T
+    def rel(a, b):
+        r = float(np.abs(a - b).max() / np.abs(b).max())
+        print(f"normwise error against fp64: {r:.3g}")
+        return r
+    assert rel(f64(acc), z) <= 1e-5
+    # bias + ReLU + bf16 rounding of the fp32 sum, exactly
+    zb = (acc.cpu().numpy() + L["b"].cpu().numpy()).astype(np.float32)
+    np.testing.assert_array_equal(f64(y), _bf16(np.maximum(zb, 0)))
+    mask = f64(y) > 0
+    g = np.where(mask, f64(dy), 0.0)
+    np.testing.assert_array_equal(f64(dz), _bf16(g))
+    assert rel(f64(gb), g.sum(axis=0)) <= 1e-5
+    dz64 = f64(dz)
+    assert rel(f64(gw)[:, :9 * cin], dz64.T @ cols_ref) <= 1e-5
+    assert not f64(gw)[:, 9 * cin:].any()
+    assert rel(f64(dx), _col2im(dz64 @ W, (n, h, h, cin))) <= 1e-5
 
 
 def test_training_lowers_the_loss():
