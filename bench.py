@@ -707,7 +707,8 @@ def main_warmstart(a, torch, dev):
     from jaxsplat_gb300.warmstart import run_experiment
 
     res = run_experiment(n_train=a.ws_train_sets, fit_steps=a.ws_fit_steps, epochs=a.ws_epochs,
-                         log=lambda m: print(m, file=sys.stderr), device=dev)
+                         log=lambda m: print(m, file=sys.stderr), device=dev,
+                         concurrent=a.ws_concurrent)
     ev = res["eval"]
     ok = all(r["learned_reached"] and r["plain_reached"] for r in ev)
     learned = float(np.mean([r["learned_s"] for r in ev]))
@@ -849,6 +850,8 @@ def main():
     ap.add_argument("--ws-train-sets", type=int, default=1000)
     ap.add_argument("--ws-fit-steps", type=int, default=300)
     ap.add_argument("--ws-epochs", type=int, default=20)
+    ap.add_argument("--ws-concurrent", type=int, default=8,
+                    help="plain fits run at once while generating the training sets")
     ap.add_argument("--autotune", action="store_true",
                     help="batch scene: sweep block size x scheduler chunk before timing")
     a = ap.parse_args()

@@ -266,30 +266,50 @@ class WarmStart:
         self.mu = np.zeros(SLOTS * NPARAM, np.float32)
         self.sd = np.ones(SLOTS * NPARAM, np.float32)
 
-    def fit_normaliser(self, grids: np.ndarray):
-        per = grids.reshape(-1, SLOTS, NPARAM)
-        mu = per.mean(axis=(0, 1))
-        sd = per.std(axis=(0, 1)) + 1e-3
-        self.mu = np.tile(mu, SLOTS).astype(np.float32)
-        self.sd = np.tile(sd, SLOTS).astype(np.float32)
+    def fit_normaliser(self, grids):
+        """Per-parameter mean and spread over every slot of every set (numpy
+        array or device tensor)."""
+        per = torch.as_tensor(grids).reshape(-1, NPARAM)
+        mu = torch.zeros(NPARAM, dtype=torch.float64, device=per.device)
+        sq = torch.zeros(NPARAM, dtype=torch.float64, device=per.device)
+        for c in torch.split(per, 1 << 22):  # in chunks: the fp64 copies stay small
+            c = c.double()
+            mu += c.sum(0)
+            sq += (c * c).sum(0)
+        n = per.shape[0]
+        mu /= n
+        sd = (sq / n - mu * mu).clamp_min(0).sqrt() + 1e-3
+        self.mu = np.tile(mu.cpu().numpy(), SLOTS).astype(np.float32)
+        self.sd = np.tile(sd.cpu().numpy(), SLOTS).astype(np.float32)
 
     def _img(self, imgs):
+        if isinstance(imgs, torch.Tensor):
+            return imgs.to(self.dev, torch.bfloat16)
         return torch.as_tensor(np.asarray(imgs, np.float32)).to(self.dev).to(torch.bfloat16)
 
     def train(self, images, grids, epochs: int = 20, batch: int = 8, lr: float = 1e-3,
               log=None) -> list:
-        """images (S, 512, 512, 3), grids (S, 1024, 224) -> per-epoch mean loss."""
+        """images (S, 512, 512, 3), grids (S, 1024, 224) (numpy arrays or
+        device tensors; a device tensor of grids is standardised in place)
+        -> per-epoch mean loss."""
         lib = _lib.load()
         self.fit_normaliser(grids)
         X = self._img(images)
-        Y = torch.as_tensor((np.asarray(grids) - self.mu) / self.sd).to(self.dev)
+        mu = torch.as_tensor(self.mu, device=self.dev)
+        sd = torch.as_tensor(self.sd, device=self.dev)
+        if isinstance(grids, torch.Tensor):
+            Y = grids.to(self.dev, torch.float32)
+            Y.sub_(mu).div_(sd)
+        else:
+            Y = (torch.as_tensor(np.asarray(grids, np.float32)).to(self.dev) - mu) / sd
         n = X.shape[0]
         loss = torch.zeros(1, device=self.dev)
+        tot = torch.zeros(1, dtype=torch.float64, device=self.dev)
         rng = np.random.default_rng(0)
         hist = []
         for ep in range(epochs):
             perm = rng.permutation(n)
-            tot = 0.0
+            tot.zero_()
             nb = n // batch
             for b in range(nb):
                 idx = torch.as_tensor(perm[b * batch:(b + 1) * batch], device=self.dev)
@@ -301,9 +321,9 @@ class WarmStart:
                            "l2_loss")
                 self.net.backward(dout)
                 self.net.adam(lr)
-                tot += float(loss.item())
+                tot += loss  # summed on the device: no host sync per step
             self.net.check()
-            hist.append(tot / max(nb, 1))
+            hist.append(float(tot.item()) / max(nb, 1))
             if log:
                 log(f"epoch {ep}: loss {hist[-1]:.4f}")
         return hist
@@ -342,36 +362,60 @@ __all__ = ["ConvNet", "WarmStart", "to_grid", "from_grid", "fit_set", "time_to_p
            "random_init"]
 
 
-def make_dataset(n_sets: int, fit_steps: int, first_seed: int = 0, device="cuda", log=None):
+def make_dataset(n_sets: int, fit_steps: int, first_seed: int = 0, device="cuda", log=None,
+                 concurrent: int = 8):
     """Targets and grid-form fitted sets of `n_sets` procedural images
     (seeds first_seed ..), each fitted by the plain loop for `fit_steps`
-    steps from random init.  One Fitter is reused (its graph stays valid)."""
+    steps from random init, kept on the device (targets as bf16, the
+    network's input type; grids as fp32).  `concurrent` fits run at once,
+    each a reused Fitter replaying its own captured step graph on its own
+    stream: one fit of 16384 Gaussians at 512x512 is a graph of small kernels
+    that leaves most of the GPU idle, and independent fits fill it."""
     from .scenes import procedural_target
 
-    imgs, grids = [], []
-    ft = None
-    for k in range(n_sets):
-        sd = first_seed + k
-        tgt = procedural_target(sd, IMG, device=device)
-        if ft is None:
-            ft = Fitter(tgt.cpu().numpy(), SLOTS * GRID * GRID, seed=sd, device=device)
-            ft.capture()
-        ft.reset(tgt, seed=sd)
-        ft.run(fit_steps)
-        ft.check()
-        if ft.graph is None:
-            ft.capture()
-        params = {kk: v.detach().cpu().numpy() for kk, v in ft.params().items()}
-        imgs.append(tgt.cpu().numpy())
-        grids.append(to_grid(params))
-        if log and (k + 1) % 100 == 0:
-            log(f"fitted {k + 1}/{n_sets}")
-    return np.stack(imgs), np.stack(grids)
+    dev = torch.device(device)
+    k_max = max(1, min(int(concurrent), n_sets))
+    fitters, streams = [], []
+    imgs = torch.empty(n_sets, IMG, IMG, 3, dtype=torch.bfloat16, device=dev)
+    grids = torch.empty(n_sets, GRID * GRID, SLOTS * NPARAM, dtype=torch.float32, device=dev)
+    cur = torch.cuda.current_stream(dev)
+    for k0 in range(0, n_sets, k_max):
+        group = list(range(k0, min(n_sets, k0 + k_max)))
+        targets = []
+        for j, k in enumerate(group):
+            sd = first_seed + k
+            tgt = procedural_target(sd, IMG, device=device)
+            if j == len(fitters):
+                fitters.append(Fitter(tgt.cpu().numpy(), SLOTS * GRID * GRID, seed=sd,
+                                      device=device))
+                streams.append(torch.cuda.Stream(dev))
+            ft = fitters[j]
+            ft.reset(tgt, seed=sd)
+            if ft.graph is None:
+                ft.capture()
+            targets.append(tgt)
+        for j in range(len(group)):
+            streams[j].wait_stream(cur)
+        for _ in range(fit_steps):
+            for j in range(len(group)):
+                with torch.cuda.stream(streams[j]):
+                    fitters[j].graph.replay()
+        for j, k in enumerate(group):
+            cur.wait_stream(streams[j])
+            ft = fitters[j]
+            ft.steps_done += fit_steps
+            ft.check()
+            params = {kk: v.detach().cpu().numpy() for kk, v in ft.params().items()}
+            imgs[k] = targets[j].to(torch.bfloat16)
+            grids[k] = torch.from_numpy(to_grid(params)).to(dev)
+        if log and (group[-1] + 1) // 100 > k0 // 100:
+            log(f"fitted {group[-1] + 1}/{n_sets}")
+    return imgs, grids
 
 
 def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
                    eval_seeds=tuple(range(1_000_000, 1_000_008)), psnr: float = 30.0,
-                   check_every: int = 5, device="cuda", log=None) -> dict:
+                   check_every: int = 5, device="cuda", log=None, concurrent: int = 8) -> dict:
     """Dataset from the plain loop, training, then wall-clock to `psnr` dB on
     held-out seeds from three starts: random init (the plain method), the
     network's proposal, and the ablation that keeps the proposal's grid
@@ -380,7 +424,7 @@ def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
     from .scenes import procedural_target
 
     t0 = time.perf_counter()
-    imgs, grids = make_dataset(n_train, fit_steps, device=device, log=log)
+    imgs, grids = make_dataset(n_train, fit_steps, device=device, log=log, concurrent=concurrent)
     t_data = time.perf_counter() - t0
     ws = WarmStart(device)
     t1 = time.perf_counter()
