@@ -708,7 +708,7 @@ def main_warmstart(a, torch, dev):
 
     res = run_experiment(n_train=a.ws_train_sets, fit_steps=a.ws_fit_steps, epochs=a.ws_epochs,
                          log=lambda m: print(m, file=sys.stderr), device=dev,
-                         concurrent=a.ws_concurrent)
+                         concurrent=a.ws_concurrent, lr=a.ws_lr)
     ev = res["eval"]
     ok = all(r["learned_reached"] and r["plain_reached"] for r in ev)
     learned = float(np.mean([r["learned_s"] for r in ev]))
@@ -849,8 +849,9 @@ def main():
                     help="batch scene: scale the scenes' Gaussian counts (profiling runs)")
     ap.add_argument("--ws-train-sets", type=int, default=1000)
     ap.add_argument("--ws-fit-steps", type=int, default=300)
-    ap.add_argument("--ws-epochs", type=int, default=20)
-    ap.add_argument("--ws-concurrent", type=int, default=8,
+    ap.add_argument("--ws-epochs", type=int, default=60)
+    ap.add_argument("--ws-lr", type=float, default=3e-3)
+    ap.add_argument("--ws-concurrent", type=int, default=16,
                     help="plain fits run at once while generating the training sets")
     ap.add_argument("--autotune", action="store_true",
                     help="batch scene: sweep block size x scheduler chunk before timing")

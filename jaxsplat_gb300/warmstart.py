@@ -413,9 +413,10 @@ def make_dataset(n_sets: int, fit_steps: int, first_seed: int = 0, device="cuda"
     return imgs, grids
 
 
-def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
+def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 60,
                    eval_seeds=tuple(range(1_000_000, 1_000_008)), psnr: float = 30.0,
-                   check_every: int = 5, device="cuda", log=None, concurrent: int = 8) -> dict:
+                   check_every: int = 5, device="cuda", log=None, concurrent: int = 16,
+                   lr: float = 3e-3) -> dict:
     """Dataset from the plain loop, training, then wall-clock to `psnr` dB on
     held-out seeds from three starts: random init (the plain method), the
     network's proposal, and the ablation that keeps the proposal's grid
@@ -428,7 +429,7 @@ def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
     t_data = time.perf_counter() - t0
     ws = WarmStart(device)
     t1 = time.perf_counter()
-    hist = ws.train(imgs, grids, epochs=epochs, log=log)
+    hist = ws.train(imgs, grids, epochs=epochs, lr=lr, log=log)
     t_train = time.perf_counter() - t1
     rows = []
     first = procedural_target(eval_seeds[0], IMG, device=device).cpu().numpy()
@@ -458,7 +459,7 @@ def run_experiment(n_train: int = 1000, fit_steps: int = 300, epochs: int = 20,
                      "mean_init_psnr": round(mean_init_psnr, 2)})
         if log:
             log(str(rows[-1]))
-    return {"train_sets": n_train, "fit_steps": fit_steps, "epochs": epochs,
+    return {"train_sets": n_train, "fit_steps": fit_steps, "epochs": epochs, "lr": lr,
             "data_s": round(t_data, 1), "train_s": round(t_train, 1),
             "loss_first": round(hist[0], 4), "loss_last": round(hist[-1], 4), "eval": rows}
 
