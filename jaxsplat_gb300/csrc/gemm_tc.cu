@@ -11,7 +11,7 @@
 // Operand tiles of 128 (or BN) rows x 64 K-elements arrive by TMA
 // (cp.async.bulk.tensor, tensor maps over this GPU's memory, no multicast)
 // in the 128-byte-swizzled K-major layout the tensor cores read directly,
-// through a ring of kGemmStages stages: thread 0 (producer) waits for a
+// through a ring of S stages: thread 0 (producer) waits for a
 // stage's "empty" barrier and issues its two tensor loads onto the stage's
 // "full" barrier; thread 32 (MMA issuer) waits for "full", issues four
 // tcgen05.mma (M 128, N BN, K 16) into a BN-column FP32 accumulator in tensor
@@ -38,16 +38,15 @@ namespace splat {
 constexpr int kGemmBM = 128;
 constexpr int kGemmBK = 64;  // 64 bf16 = one 128-byte swizzle row
 constexpr int kGemmThreads = 128;
-constexpr int kGemmStages = 4;
 constexpr int kGemmATile = kGemmBM * kGemmBK * 2;  // 16 KB
 
 template <int BN>
 constexpr int gemm_stage_bytes() {
     return kGemmATile + BN * kGemmBK * 2;
 }
-template <int BN>
+template <int BN, int S>
 constexpr int gemm_smem() {
-    return kGemmStages * gemm_stage_bytes<BN>() + 1024;  // + alignment slack
+    return S * gemm_stage_bytes<BN>() + 1024;  // + alignment slack
 }
 
 enum GemmOut { kOutF32 = 0, kOutBiasBF16 = 1, kOutBiasF32 = 2 };
@@ -127,9 +126,10 @@ struct GemmArgs {
     uint32_t spin_limit;
 };
 
-// Epilogue of one row segment of 16 accumulator columns starting at column n.
+// Epilogue of one row segment of 16 accumulator columns starting at column n;
+// bias16 = the bias of those columns (shared memory).
 __device__ __forceinline__ void gemm_store16(const GemmArgs &a, int row, int n, const uint32_t r[16],
-                                             bool split) {
+                                             bool split, const float *bias16) {
     if (a.mode == kOutF32) {
         float *crow = a.C + (size_t)row * a.ldc;
 #pragma unroll
@@ -144,8 +144,7 @@ __device__ __forceinline__ void gemm_store16(const GemmArgs &a, int row, int n, 
     float v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-        const int c = min(n + q, a.N - 1);
-        v[q] = __uint_as_float(r[q]) + a.bias[c];
+        v[q] = __uint_as_float(r[q]) + bias16[q];
         if (a.relu) v[q] = fmaxf(v[q], 0.f);
     }
     if (a.mode == kOutBiasF32) {
@@ -174,16 +173,18 @@ __device__ __forceinline__ void gemm_store16(const GemmArgs &a, int row, int n, 
     }
 }
 
-template <int BN>
+template <int BN, int S>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     gemm_bf16_tc_kernel(const __grid_constant__ CUtensorMap map_a,
                         const __grid_constant__ CUtensorMap map_b, GemmArgs a) {
     constexpr uint32_t kStage = (uint32_t)gemm_stage_bytes<BN>();
+    static_assert(gemm_smem<BN, S>() <= 227 * 1024, "stage ring exceeds shared memory");
     extern __shared__ uint8_t g_dyn[];
-    __shared__ __align__(8) uint64_t s_full[kGemmStages];
-    __shared__ __align__(8) uint64_t s_empty[kGemmStages];
+    __shared__ __align__(8) uint64_t s_full[S];
+    __shared__ __align__(8) uint64_t s_empty[S];
     __shared__ __align__(8) uint64_t s_done;
     __shared__ uint32_t s_tmem;
+    __shared__ float s_bias[BN];  // this tile's bias columns (zero past N)
     // 1024-byte aligned stage buffers (the swizzle atoms)
     const uint32_t base = (smem_addr(g_dyn) + 1023u) & ~1023u;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (t == 0) {
-        for (int s = 0; s < kGemmStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_full[s]))
                          : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_empty[s]))
@@ -212,6 +213,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
         asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
     }
+    if (a.mode != kOutF32)
+        for (int c = t; c < BN; c += kGemmThreads) s_bias[c] = n0 + c < a.N ? a.bias[n0 + c] : 0.f;
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -223,9 +226,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     bool ok = true;
     if (ktiles > 0 && t == 0) {  // producer: TMA loads into the ring
         for (int kt = 0; kt < ktiles; ++kt) {
-            const int s = kt % kGemmStages;
-            if (kt >= kGemmStages &&
-                !mbar_wait(smem_addr(&s_empty[s]), (uint32_t)((kt / kGemmStages - 1) & 1),
+            const int s = kt % S;
+            if (kt >= S &&
+                !mbar_wait(smem_addr(&s_empty[s]), (uint32_t)((kt / S - 1) & 1),
                            a.spin_limit)) {
                 ok = false;
                 break;
@@ -240,8 +243,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     } else if (ktiles > 0 && t == 32) {  // MMA issuer
         const uint32_t idesc = mma_idesc(kGemmBM, BN);
         for (int kt = 0; kt < ktiles; ++kt) {
-            const int s = kt % kGemmStages;
-            if (!mbar_wait(smem_addr(&s_full[s]), (uint32_t)((kt / kGemmStages) & 1),
+            const int s = kt % S;
+            if (!mbar_wait(smem_addr(&s_full[s]), (uint32_t)((kt / S) & 1),
                            a.spin_limit)) {
                 ok = false;
                 break;
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 : "r"(lane_addr + (uint32_t)c)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if (row < a.M && n0 + c < a.N) gemm_store16(a, row, n0 + c, r, split);
+            if (row < a.M && n0 + c < a.N) gemm_store16(a, row, n0 + c, r, split, s_bias + c);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -348,16 +351,26 @@ static int make_operand_map(CUtensorMap *map, const void *ptr, int rows, int k, 
     return SPLAT_OK;
 }
 
+template <int BN, int S>
+static int launch_gemm(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, dim3 grid,
+                       cudaStream_t stream) {
+    auto kernel = gemm_bf16_tc_kernel<BN, S>;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             gemm_smem<BN, S>()) != cudaSuccess)
+        return check_launch("gemm shared-memory attribute");
+    kernel<<<grid, kGemmThreads, gemm_smem<BN, S>(), stream>>>(ma, mb, g);
+    return check_launch("gemm_bf16_tc_kernel");
+}
+
+// The ring depth follows the K tiles a CTA walks: 2 stages when it walks at
+// most 2 (the shared memory left lets more CTAs share an SM), else 6 (more
+// tensor loads in flight for a CTA that is alone on its SM and waits on them).
 template <int BN>
 static int launch_gemm(const void *A, const void *B, GemmArgs g, int lda, int ldb,
                        cudaStream_t stream) {
     alignas(64) CUtensorMap ma, mb;
     if (int rc = make_operand_map(&ma, A, g.M, g.K, lda, kGemmBM)) return rc;
     if (int rc = make_operand_map(&mb, B, g.N, g.K, ldb, BN)) return rc;
-    auto kernel = gemm_bf16_tc_kernel<BN>;
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             gemm_smem<BN>()) != cudaSuccess)
-        return check_launch("gemm shared-memory attribute");
     const int gm = (g.M + kGemmBM - 1) / kGemmBM, gn = (g.N + BN - 1) / BN;
     const int kt_total = (g.K + kGemmBK - 1) / kGemmBK;
     // split K (kOutF32 only) when the output has few tiles and K is long:
@@ -372,9 +385,9 @@ static int launch_gemm(const void *A, const void *B, GemmArgs g, int lda, int ld
         cudaMemset2DAsync(g.C, sizeof(float) * (size_t)g.ldc, 0, sizeof(float) * (size_t)g.N,
                           (size_t)g.M, stream) != cudaSuccess)
         return check_launch("gemm split-K zero");
-    dim3 grid(gm, gn, splits);
-    kernel<<<grid, kGemmThreads, gemm_smem<BN>(), stream>>>(ma, mb, g);
-    return check_launch("gemm_bf16_tc_kernel");
+    const dim3 grid(gm, gn, splits);
+    return g.ktiles_per <= 2 ? launch_gemm<BN, 2>(ma, mb, g, grid, stream)
+                             : launch_gemm<BN, 6>(ma, mb, g, grid, stream);
 }
 
 static int check_operands(const void *A, const void *B, int M, int N, int K, int lda, int ldb) {
