@@ -362,9 +362,14 @@ static int launch_gemm(const CUtensorMap &ma, const CUtensorMap &mb, const GemmA
     return check_launch("gemm_bf16_tc_kernel");
 }
 
-// The ring depth follows the K tiles a CTA walks: 2 stages when it walks at
-// most 2 (the shared memory left lets more CTAs share an SM), else 6 (more
-// tensor loads in flight for a CTA that is alone on its SM and waits on them).
+// The ring depth follows the K tiles a CTA walks and what shares its SM: 2
+// stages when it walks at most 2 (the shared memory left lets more CTAs share
+// an SM); 6 (more tensor loads in flight) when that costs no resident CTA --
+// 128-column tiles are one per SM at 4 stages already -- or the grid fits
+// one wave; else 4, which keeps two 32- or 64-column CTAs per SM.  Measured
+// on the network's forward: the first layer (1 K tile) 43.2 -> 31.6 us with
+// 2 stages; 128-column layers 20.1 -> 18.4 and 15.4 -> 13.6 us with 6; a
+// 64-column layer of 1024 CTAs 30.6 -> 38.6 us with 6, hence 4 there.
 template <int BN>
 static int launch_gemm(const void *A, const void *B, GemmArgs g, int lda, int ldb,
                        cudaStream_t stream) {
@@ -386,8 +391,10 @@ static int launch_gemm(const void *A, const void *B, GemmArgs g, int lda, int ld
                           (size_t)g.M, stream) != cudaSuccess)
         return check_launch("gemm split-K zero");
     const dim3 grid(gm, gn, splits);
-    return g.ktiles_per <= 2 ? launch_gemm<BN, 2>(ma, mb, g, grid, stream)
-                             : launch_gemm<BN, 6>(ma, mb, g, grid, stream);
+    if (g.ktiles_per <= 2) return launch_gemm<BN, 2>(ma, mb, g, grid, stream);
+    if (BN == 128 || (long long)gm * gn * splits <= 152)
+        return launch_gemm<BN, 6>(ma, mb, g, grid, stream);
+    return launch_gemm<BN, 4>(ma, mb, g, grid, stream);
 }
 
 static int check_operands(const void *A, const void *B, int M, int N, int K, int lda, int ldb) {

@@ -169,17 +169,18 @@ def test_training_lowers_the_loss():
 def test_learned_warm_start_beats_plain_fit():
     """The learned part's gain over the plain method and over its ablation.
     A network trained on 1000 fits of the plain loop (300 Adam steps each,
-    60 epochs) proposes initial Gaussians for held-out targets; wall-clock
+    60 epochs) proposes initial Gaussians for 8 held-out targets; wall-clock
     to 30 dB PSNR (proposal, loading and fitting included) is compared with
     (a) the plain loop from random init: at most 0.25x (the target; measured
-    0.20x at this size, 0.25x with 20 epochs), and (b) the ablation that keeps
+    0.20x at this size on these seeds, 0.25x with 20 epochs, 0.21-0.23x on
+    their first four alone), and (b) the ablation that keeps
     the proposal's grid layout and dataset-mean slot parameters but ignores
     the image: at most 0.6x (measured ~0.26x), so the gain is what the network
     reads in the image, not the fixed grid prior."""
     from jaxsplat_gb300.warmstart import run_experiment
 
     r = run_experiment(n_train=1000, fit_steps=300, epochs=60, lr=3e-3,
-                       eval_seeds=(1_000_000, 1_000_001, 1_000_002, 1_000_003), check_every=5)
+                       eval_seeds=tuple(range(1_000_000, 1_000_008)), check_every=5)
     assert r["loss_last"] < r["loss_first"]
     for row in r["eval"]:
         assert row["plain_reached"] and row["learned_reached"] and row["mean_reached"], row
