@@ -673,12 +673,12 @@ def add_compute_roofline(line, st):
         ms = line["stages_ms"][dom]
         hbm = {k: line["roofline"][k] for k in ("achieved", "peak", "unit", "frac", "peak_source")}
         if b == "fp32":
-            achieved, peak, unit = flops[dom] / (ms * 1e-3) / 1e12, fp32 / 1e12, "TFLOP/s"
+            achieved, cpeak, unit = flops[dom] / (ms * 1e-3) / 1e12, fp32 / 1e12, "TFLOP/s"
         else:
-            achieved, peak, unit = sfu[dom] / (ms * 1e-3) / 1e12, ex2 / 1e12, "Tex2/s"
+            achieved, cpeak, unit = sfu[dom] / (ms * 1e-3) / 1e12, ex2 / 1e12, "Tex2/s"
         line["roofline"].update({
-            "bound": b, "achieved": round(achieved, 3), "peak": round(peak, 2), "unit": unit,
-            "frac": round(achieved / peak, 4),
+            "bound": b, "achieved": round(achieved, 3), "peak": round(cpeak, 2), "unit": unit,
+            "frac": round(achieved / cpeak, 4),
             "peak_source": f"nominal per-SM rate x {sms} SMs x {clk:.0f} MHz (sampled)",
             "algorithmic_flops" if b == "fp32" else "algorithmic_ex2":
                 flops[dom] if b == "fp32" else sfu[dom],

@@ -502,21 +502,18 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
         __syncthreads();
         const int n = min(kF16Batch, range.y - start);
         const int cnt = warp_list(s_mask, 0, n, warp, lane, 0xffffffffu, s_list[warp]);
-        for (int k = 0; k < cnt; ++k) {
-            const int t = s_list[warp][k];
-            const float4 r0 = s_r0[t];
-            const float4 r1 = s_r1[t];
-            const float dx = r0.x - px;
-            const float2 dy = add2(f2(r0.y), neg_py);
-            const float2 sigma = falloff2(r0.z, r0.w, r1.x, dx, dy);
-            const float2 ov = mul2(f2(r1.y), make_float2(__expf(-sigma.x), __expf(-sigma.y)));
+        // Two list entries per iteration: both entries' falloffs and
+        // exponentials are independent and go first, the blends follow in
+        // list order (the arithmetic per entry is unchanged).
+        // blend_entry: the blend of one entry whose falloff and opacity x
+        // exponent are known; returns true when every pixel of the warp is
+        // saturated.
+        auto blend_entry = [&](int t, const float4 &r1, float2 sigma, float2 ov) -> bool {
             const float al0 = fminf(0.999f, ov.x), al1 = fminf(0.999f, ov.y);
             const bool pass0 = !done0 && !(sigma.x < 0.f || al0 < 1.f / 255.f);
             const bool pass1 = !done1 && !(sigma.y < 0.f || al1 < 1.f / 255.f);
-            if (!__any_sync(0xffffffffu, pass0 || pass1)) {
-                if (__all_sync(0xffffffffu, done0 && done1)) break;
-                continue;
-            }
+            if (!__any_sync(0xffffffffu, pass0 || pass1))
+                return __all_sync(0xffffffffu, done0 && done1);
             const float2 al = make_float2(pass0 ? al0 : 0.f, pass1 ? al1 : 0.f);
             const float2 next_T = mul2(T, fma2(al, f2(-1.f), f2(1.f)));  // T (1 - alpha)
             // a pixel whose next T would fall to 1e-4 stops before this
@@ -537,6 +534,31 @@ __device__ __forceinline__ void fwd16_tile(const RasterFwdArgs &a, const TileCtx
             if (bl1) cur1 = start + t;
             done0 |= stop0;
             done1 |= stop1;
+            return false;
+        };
+        auto eval = [&](const float4 &r0, const float4 &r1, float2 &sigma, float2 &ov) {
+            const float dx = r0.x - px;
+            const float2 dy = add2(f2(r0.y), neg_py);
+            sigma = falloff2(r0.z, r0.w, r1.x, dx, dy);
+            ov = mul2(f2(r1.y), make_float2(__expf(-sigma.x), __expf(-sigma.y)));
+        };
+        int k = 0;
+        bool warp_done = false;
+        for (; k + 1 < cnt; k += 2) {
+            const int ta = s_list[warp][k], tb = s_list[warp][k + 1];
+            const float4 r0a = s_r0[ta], r1a = s_r1[ta], r0b = s_r0[tb], r1b = s_r1[tb];
+            float2 sa, oa, sb, ob;
+            eval(r0a, r1a, sa, oa);
+            eval(r0b, r1b, sb, ob);
+            if ((warp_done = blend_entry(ta, r1a, sa, oa))) break;
+            if ((warp_done = blend_entry(tb, r1b, sb, ob))) break;
+        }
+        if (!warp_done && k < cnt) {
+            const int t = s_list[warp][k];
+            const float4 r0 = s_r0[t], r1 = s_r1[t];
+            float2 sg, o;
+            eval(r0, r1, sg, o);
+            blend_entry(t, r1, sg, o);
         }
         if (kBlend) {
             prev_start = start;
