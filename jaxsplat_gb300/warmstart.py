@@ -18,7 +18,7 @@ placeholders) -- and the network regresses the standardised per-slot
 parameters (centre offset within the cell in cell units, depth, |scales|,
 sign-normalised unit quaternion, raw colours, raw opacity) with an MSE loss.
 
-Plain fitting from random init stays both the fallback and the judge: the
+Plain fitting from random init stays both the fallback and the yardstick: the
 measurement is wall-clock to 30 dB PSNR from the network's proposal versus
 from random init, on held-out seeds.
 """

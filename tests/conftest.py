@@ -49,7 +49,7 @@ def load_small_digests() -> dict:
         return json.load(fh)
 
 
-# Output groups and their parity bar (the benchmark spec): integer/index outputs
+# Output groups and their parity bar: integer/index outputs
 # bit-exact; image within 1e-5 absolute; gradients within 1e-4 relative
 # (normwise: max |a - b| / max |b|).
 INT_KEYS = ["radii", "num_tiles_hit", "cum_tiles_hit", "isect_ids", "gaussian_ids",
