@@ -72,6 +72,57 @@ __device__ __forceinline__ unsigned long long block_scan(unsigned long long v,
     return r;
 }
 
+// Projects Gaussian i and writes every output of it (forward.cu:37-116; the
+// reference's memsets provide the zeros of culled Gaussians); returns its
+// tile count.
+__device__ __forceinline__ uint32_t project_store(const ProjFwdArgs &a, const ProjCam &cam, int i) {
+    const ProjOut o = project_one(cam, a.means3d + 3 * (size_t)i, a.scales + 3 * (size_t)i,
+                                  a.quats + 4 * (size_t)i);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a.cov3d[6 * (size_t)i + k] = o.cov[k];
+    a.xys[2 * (size_t)i] = o.center.x;
+    a.xys[2 * (size_t)i + 1] = o.center.y;
+    a.depths[i] = o.depth;
+    a.radii[i] = o.radius;
+    a.conics[3 * (size_t)i] = o.conic.x;
+    a.conics[3 * (size_t)i + 1] = o.conic.y;
+    a.conics[3 * (size_t)i + 2] = o.conic.z;
+    a.comp[i] = o.comp;
+    a.ntiles[i] = (int32_t)o.hits;
+    if (a.rec)
+        write_record(a.rec + 3 * (size_t)i, o.center, o.conic, a.opac[i],
+                     make_float3(a.colors[3 * (size_t)i], a.colors[3 * (size_t)i + 1],
+                                 a.colors[3 * (size_t)i + 2]),
+                     0.f);
+    return o.hits;
+}
+
+// Without cum_tiles_hit only the intersection total is wanted: one Gaussian
+// per thread, no scan and no partition order, the block's tile counts summed
+// (warp reductions, then one 64-bit atomic per block).
+constexpr int kProjTotalThreads = 256;
+
+__global__ void __launch_bounds__(kProjTotalThreads) project_fwd_total_kernel(ProjFwdArgs a) {
+    __shared__ unsigned s_warp[kProjTotalThreads / 32];
+    const ProjCam cam{a.viewmat, a.glob_scale, a.fx, a.fy, a.cx, a.cy, a.tanx, a.tany,
+                      a.clip, a.tiles_x, a.tiles_y, a.bw};
+    const int i = blockIdx.x * kProjTotalThreads + threadIdx.x;
+    const uint32_t hits = i < a.n ? project_store(a, cam, i) : 0u;
+    const unsigned w = __reduce_add_sync(0xffffffffu, hits);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long sum = 0;
+#pragma unroll
+        for (int k = 0; k < kProjTotalThreads / 32; ++k) sum += s_warp[k];
+        if (sum) {
+            const unsigned long long old =
+                atomicAdd(reinterpret_cast<unsigned long long *>(a.total), sum);
+            if (old + sum > 0x7fffffffull) raise_status(a.status, DEV_SCAN_OVERFLOW);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a) {
     __shared__ int s_part;
     __shared__ unsigned long long s_warp[kProjWarps];
@@ -91,41 +142,11 @@ __global__ void __launch_bounds__(kProjThreads) project_fwd_kernel(ProjFwdArgs a
     for (int r = 0; r < kProjRounds; ++r) {
         if (r >= a.rounds) break;
         const int i = part * part_size + r * kProjThreads + threadIdx.x;
-        uint32_t hits = 0;
-        if (i < a.n) {
-            const ProjOut o = project_one(cam, a.means3d + 3 * (size_t)i, a.scales + 3 * (size_t)i,
-                                          a.quats + 4 * (size_t)i);
-            hits = o.hits;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) a.cov3d[6 * (size_t)i + k] = o.cov[k];
-            a.xys[2 * (size_t)i] = o.center.x;
-            a.xys[2 * (size_t)i + 1] = o.center.y;
-            a.depths[i] = o.depth;
-            a.radii[i] = o.radius;
-            a.conics[3 * (size_t)i] = o.conic.x;
-            a.conics[3 * (size_t)i + 1] = o.conic.y;
-            a.conics[3 * (size_t)i + 2] = o.conic.z;
-            a.comp[i] = o.comp;
-            a.ntiles[i] = (int32_t)hits;
-            if (a.rec)
-                write_record(a.rec + 3 * (size_t)i, o.center, o.conic, a.opac[i],
-                             make_float3(a.colors[3 * (size_t)i], a.colors[3 * (size_t)i + 1],
-                                         a.colors[3 * (size_t)i + 2]),
-                             0.f);
-        }
+        const uint32_t hits = i < a.n ? project_store(a, cam, i) : 0u;
         unsigned long long round_total;
         incl[r] = run + block_scan(hits, s_warp, &round_total);
         run += round_total;
     }
-    if (a.cum == nullptr) {  // only the total is wanted: one atomic per block
-        if (threadIdx.x == 0 && run) {
-            const unsigned long long old =
-                atomicAdd(reinterpret_cast<unsigned long long *>(a.total), run);
-            if (old + run > 0x7fffffffull) raise_status(a.status, DEV_SCAN_OVERFLOW);
-        }
-        return;
-    }
-
     // partition prefix by decoupled look-back (64-bit carries)
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
@@ -233,6 +254,11 @@ int launch_project_fwd(const splat_params &p, const float *means3d, const float 
     a.spin_limit = spin_limit(p);
     a.rounds = rounds;
     a.colors = colors; a.opac = opac; a.rec = reinterpret_cast<float4 *>(rec);
+    if (!cum) {
+        project_fwd_total_kernel<<<(n + kProjTotalThreads - 1) / kProjTotalThreads,
+                                   kProjTotalThreads, 0, s>>>(a);
+        return check_launch("project_fwd_total_kernel");
+    }
     project_fwd_kernel<<<nparts, kProjThreads, 0, s>>>(a);
     return check_launch("project_fwd_kernel");
 }
