@@ -1,7 +1,7 @@
 """Benchmark: forward+backward of the render path, 1M Gaussians at 1920x1080.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--scene hd|uhd|small|batch|fit|warmstart] [--no-cpu-baseline]
+                    [--scene hd|uhd|small|batch|fit|warmstart|netstep] [--no-cpu-baseline]
 
 One step = project -> sort/bin -> rasterize forward with the L2 loss against
 a target image -> rasterize backward -> project backward (one CUDA graph, the
@@ -726,6 +726,82 @@ def main_warmstart(a, torch, dev):
                       "experiment": res}))
 
 
+NET_METRIC = "warm-start network training step (fwd + bwd + Adam) ms/iter, batch 8, 512x512"
+
+
+def main_netstep(a, torch, dev):
+    """--scene netstep: one training step of the warm-start network (the
+    four im2col + tcgen05 GEMM convolutions and the head, the L2 loss, the
+    backward with MN-major weight- and data-gradient GEMMs and the fused
+    col2im + ReLU gradient, one Adam launch) on seeded random 512x512 images
+    and targets resident on the device, batches of 8 cycling through 64."""
+    import ctypes as C
+
+    from jaxsplat_gb300 import _lib
+    from jaxsplat_gb300.warmstart import IMG, NPARAM, SLOTS, ConvNet, _p
+
+    lib = _lib.load()
+    net = ConvNet(dev, seed=a.seed)
+    g = torch.Generator(device="cpu").manual_seed(a.seed)
+    pool, B = 64, 8
+    X = torch.rand(pool, IMG, IMG, 3, generator=g).to(dev).to(torch.bfloat16)
+    Y = torch.randn(pool, 32 * 32 * SLOTS * NPARAM, generator=g).to(dev)
+    loss = torch.zeros(1, device=dev)
+
+    def step(i):
+        idx = torch.arange((i * B) % pool, (i * B) % pool + B, device=dev)
+        out = net.forward(X[idx])
+        dout = torch.empty_like(out)
+        tgt = Y[idx].reshape(-1, SLOTS * NPARAM)
+        _lib.check(lib.splat_l2_loss(_p(out), _p(tgt), out.numel(), _p(loss), _p(dout),
+                                     C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
+                   "l2_loss")
+        net.backward(dout)
+        net.adam(1e-3)
+
+    for i in range(a.warmup):
+        step(i)
+    net.check()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(a.steps):
+        step(a.warmup + i)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    assert int(net.status.item()) == 0, "a tensor-core wait ran out"
+    # GEMM FLOPs per step: forward, weight gradients, data gradients (not the
+    # first layer's input)
+    flops, h = 0, IMG
+    for k, L in enumerate(net.layers):
+        h = (h - 1) // 2 + 1
+        P = B * h * h
+        flops += 2 * P * L["k"] * L["cout"] * (2 if k == 0 else 3)
+    Hd = net.head
+    flops += 3 * 2 * B * 32 * 32 * Hd["k"] * Hd["cout"]
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            bf16_peak = float(json.load(fh)["bf16_tflops"])
+    except Exception:
+        bf16_peak = None
+    tf = flops / (ms * 1e-3) / 1e12
+    # libsplat kernels per step: 4 im2col + 14 GEMM + loss + 2 act_grad +
+    # 3 col2im_act + 1 Adam
+    per_step = 25
+    print(json.dumps({"metric": NET_METRIC, "value": round(ms, 4), "unit": "ms",
+                      "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+                      "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "bf16 operands, f32 accumulation", "data": "synthetic (seeded)",
+                      "config": {"workload": "warm-start network: conv 3-32-64-128-256 + 1x1 head "
+                                             "to 32x32x16x14, batch 8 of 512x512",
+                                 "l2": "inputs (64 x 1.5 MB images) cycle through L2"},
+                      "gemm_gflop_per_step": round(flops / 1e9, 2),
+                      "gemm_tflops": round(tf, 1),
+                      "bf16_peak_tflops": bf16_peak,
+                      "gpu_launches": per_step * a.steps}))
+
+
 def main_fit(a, torch, dev):
     """--scene fit: wall-clock of the plain fitting loop (random init, Adam
     lr 1e-2, one CUDA graph per step, PSNR checked every 25 steps) until the
@@ -879,6 +955,8 @@ def main():
         return main_fit(a, torch, dev)
     if a.scene == "warmstart":
         return main_warmstart(a, torch, dev)
+    if a.scene == "netstep":
+        return main_netstep(a, torch, dev)
     sc = make_scene(a.scene, seed=a.seed)
     config = {"workload": f"{sc.spec.name}: {sc.spec.num_points} Gaussians, "
                           f"{sc.spec.img_shape[1]}x{sc.spec.img_shape[0]}, block 16, fp32, "

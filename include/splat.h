@@ -483,6 +483,16 @@ SPLAT_API int splat_batch_project_bwd(const splat_batch *b, const float *means3d
 SPLAT_API int splat_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int lda,
                               int ldb, int ldc, int accumulate, uint32_t *status_dev,
                               splat_stream_t stream);
+/* The same product with either operand stored MN-major (transposed):
+ *   a_mn = 0: A stored [M,K] (lda >= K);  a_mn = 1: A stored [K,M] (lda >= M),
+ *   b_mn = 0: B stored [N,K] (ldb >= K);  b_mn = 1: B stored [K,N] (ldb >= N),
+ *   C[M,N] = op(A) x op(B)^T (+ C when accumulate), op(A) = [M,K], op(B) = [N,K].
+ * The weight gradient of a convolution (a reduction over pixel rows, both
+ * operands MN-major) and its data gradient (the weights as stored, B
+ * MN-major) need no transposed copies.  Operand rules as splat_gemm_bf16. */
+SPLAT_API int splat_gemm_bf16_mn(const void *A, int a_mn, const void *B, int b_mn, float *C, int M,
+                                 int N, int K, int lda, int ldb, int ldc, int accumulate,
+                                 uint32_t *status_dev, splat_stream_t stream);
 /* The same product with the bias, the activation and the output conversion
  * in the GEMM's epilogue (the fp32 product is never stored):
  *   y[M,N] = act(A[M,K] x B[N,K]^T + bias[N]), act = ReLU when relu != 0,
@@ -496,8 +506,13 @@ SPLAT_API int splat_gemm_bf16_bias_act(const void *A, const void *B, const float
  * (padding 1, stride 1 or 2) on NHWC bf16 activations; no counterpart in the
  * reference.
  *   im2col3x3: x (n,h,w,c) bf16 -> cols (n*ho*wo, kpad) bf16, column
- *     (ky*3 + kx)*c + ch, zeros past 9c (kpad >= 9c, a multiple of 8)
+ *     (ky*3 + kx)*c + ch, zeros past 9c (kpad >= 9c, a multiple of 8; cols
+ *     16-byte aligned; n*h*w*c < 2^31)
  *   col2im3x3: dcols (n*ho*wo, kpad) fp32 -> dx (n,h,w,c) fp32 (overwritten)
+ *   col2im_act3x3: the same gather through the previous layer's ReLU:
+ *     dz (n,h,w,c) bf16 = dx * [y > 0] (y: that layer's bf16 output, NHWC),
+ *     dbias (c) += dz's channel sums; c and kpad multiples of 4, c <= 4096,
+ *     dcols 16-byte and y, dz 8-byte aligned
  *   bias_act:  y = act(acc + bias) (ReLU when relu != 0), rows x cols, to y
  *     (bf16) and/or y32 (fp32)
  *   act_grad:  dz = dy * [y > 0] (or dy) as bf16; dbias += column sums
@@ -508,6 +523,9 @@ SPLAT_API int splat_nn_im2col3x3(const void *x, void *cols, int n, int h, int w,
                                  int kpad, splat_stream_t stream);
 SPLAT_API int splat_nn_col2im3x3(const float *dcols, float *dx, int n, int h, int w, int c,
                                  int stride, int kpad, splat_stream_t stream);
+SPLAT_API int splat_nn_col2im_act3x3(const float *dcols, const void *y, void *dz, float *dbias,
+                                     int n, int h, int w, int c, int stride, int kpad,
+                                     splat_stream_t stream);
 SPLAT_API int splat_nn_bias_act(const float *acc, const float *bias, void *y, float *y32,
                                 int64_t rows, int cols, int relu, splat_stream_t stream);
 SPLAT_API int splat_nn_act_grad(const float *dy, const void *y, void *dz, float *dbias,
@@ -516,6 +534,16 @@ SPLAT_API int splat_nn_transpose_bf16(const void *in, void *out, int64_t rows, i
                                       int64_t ld_out, splat_stream_t stream);
 SPLAT_API int splat_nn_adam(float *w, float *m, float *v, const float *g, void *w16, int64_t n,
                             float lr, int step, splat_stream_t stream);
+/* Adam over up to 16 parameter arrays in one launch (each as splat_nn_adam;
+ * w16 optional per array; an empty array may have NULL pointers). */
+typedef struct splat_adam_seg {
+    float *w, *m, *v;
+    const float *g;
+    void *w16;
+    int64_t n;
+} splat_adam_seg;
+SPLAT_API int splat_nn_adam_multi(const splat_adam_seg *segs, int nseg, float lr, int step,
+                                  splat_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Self-test of the bounded wait: one block waits on a flag that nothing

@@ -65,6 +65,15 @@ class SplatBatch(C.Structure):
     ]
 
 
+class SplatAdamSeg(C.Structure):
+    """Mirror of ``splat_adam_seg`` (include/splat.h)."""
+
+    _fields_ = [
+        ("w", C.c_void_p), ("m", C.c_void_p), ("v", C.c_void_p), ("g", C.c_void_p),
+        ("w16", C.c_void_p), ("n", C.c_int64),
+    ]
+
+
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "workspace too small",
           4: "intersection count out of range", 5: "device-side check failed"}
 
@@ -118,13 +127,16 @@ _SIGS = [
     ("splat_batch_l2_loss", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 4 + [_v]),
     ("splat_batch_project_bwd", C.c_int, [C.POINTER(SplatBatch)] + [_v] * 12 + [_v]),
     ("splat_gemm_bf16", C.c_int, [_v, _v, _v] + [C.c_int] * 7 + [_v, _v]),
+    ("splat_gemm_bf16_mn", C.c_int, [_v, C.c_int, _v, C.c_int, _v] + [C.c_int] * 7 + [_v, _v]),
     ("splat_gemm_bf16_bias_act", C.c_int, [_v] * 5 + [C.c_int] * 7 + [_v, _v]),
     ("splat_nn_im2col3x3", C.c_int, [_v, _v] + [C.c_int] * 6 + [_v]),
     ("splat_nn_col2im3x3", C.c_int, [_v, _v] + [C.c_int] * 6 + [_v]),
+    ("splat_nn_col2im_act3x3", C.c_int, [_v, _v, _v, _v] + [C.c_int] * 6 + [_v]),
     ("splat_nn_bias_act", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),
     ("splat_nn_act_grad", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),
     ("splat_nn_transpose_bf16", C.c_int, [_v, _v, C.c_int64, C.c_int, C.c_int64, _v]),
     ("splat_nn_adam", C.c_int, [_v, _v, _v, _v, _v, C.c_int64, C.c_float, C.c_int, _v]),
+    ("splat_nn_adam_multi", C.c_int, [C.POINTER(SplatAdamSeg), C.c_int, C.c_float, C.c_int, _v]),
 ]
 
 EXPORTED = [name for name, _, _ in _SIGS]

@@ -69,6 +69,25 @@ class ConvNet:
         wh = torch.randn(SLOTS * NPARAM, CHANNELS[-1], generator=g) * math.sqrt(1.0 / CHANNELS[-1])
         self.head = self._param(wh, torch.zeros(SLOTS * NPARAM), CHANNELS[-1], SLOTS * NPARAM,
                                 CHANNELS[-1])
+        # the bias gradients (accumulated by atomics) share one buffer, zeroed
+        # once per backward; the weight gradients are overwritten by their GEMMs
+        params = self.layers + [self.head]
+        self.gb_flat = torch.zeros(sum(prm["b"].numel() for prm in params), device=self.dev)
+        off = 0
+        for prm in params:
+            nb = prm["b"].numel()
+            prm["gb"] = self.gb_flat[off:off + nb]
+            off += nb
+        # every weight and bias array as one segment of a single Adam launch
+        segs = []
+        for prm in params:
+            segs.append(_lib.SplatAdamSeg(prm["w"].data_ptr(), prm["mw"].data_ptr(),
+                                          prm["vw"].data_ptr(), prm["gw"].data_ptr(),
+                                          prm["w16"].data_ptr(), prm["w"].numel()))
+            segs.append(_lib.SplatAdamSeg(prm["b"].data_ptr(), prm["mb"].data_ptr(),
+                                          prm["vb"].data_ptr(), prm["gb"].data_ptr(), None,
+                                          prm["b"].numel()))
+        self._adam_segs = (_lib.SplatAdamSeg * len(segs))(*segs)
         self.step_count = 0
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
 
@@ -87,6 +106,13 @@ class ConvNet:
     def gemm(self, A, B, Cm, M, N, K, lda, ldb, ldc, acc=False):
         _lib.check(self.lib.splat_gemm_bf16(_p(A), _p(B), _p(Cm), M, N, K, lda, ldb, ldc, int(acc),
                                             _p(self.status), self._s()), "gemm_bf16")
+
+    def gemm_mn(self, A, a_mn, B, b_mn, Cm, M, N, K, lda, ldb, ldc):
+        """Cm = op(A) op(B)^T with A stored [K, M] when a_mn (else [M, K]) and
+        B stored [K, N] when b_mn (else [N, K])."""
+        _lib.check(self.lib.splat_gemm_bf16_mn(_p(A), int(a_mn), _p(B), int(b_mn), _p(Cm), M, N, K,
+                                               lda, ldb, ldc, 0, _p(self.status), self._s()),
+                   "gemm_bf16_mn")
 
     def gemm_bias_act(self, A, B, bias, M, N, K, relu, bf16_out=True):
         """act(A B^T + bias) with the bias, ReLU and output conversion fused
@@ -136,45 +162,43 @@ class ConvNet:
         B = self.batch
         Hd = self.head
         P = dout.shape[0]
-        for prm in self.layers + [Hd]:
-            prm["gw"].zero_()
-            prm["gb"].zero_()
+        self.gb_flat.zero_()
         dz = torch.empty(P, Hd["cout"], dtype=torch.bfloat16, device=self.dev)
         _lib.check(lib.splat_nn_act_grad(_p(dout), None, _p(dz), _p(Hd["gb"]), P, Hd["cout"], 0, s),
                    "act_grad")
-        # dWh = dz^T y4 ; dy4 = dz Wh
-        self.gemm(self.transpose(dz, P, Hd["cout"]), self.transpose(self.head_in, P, Hd["k"]),
-                  Hd["gw"], Hd["cout"], Hd["k"], P, P, P, Hd["k"])
+        # dWh = dz^T y4 (both stored pixel-major: MN-major operands);
+        # dy4 = dz Wh (Wh as stored: MN-major B)
+        self.gemm_mn(dz, True, self.head_in, True, Hd["gw"], Hd["cout"], Hd["k"], P,
+                     Hd["cout"], Hd["k"], Hd["k"])
         dy = torch.empty(P, Hd["k"], device=self.dev)
-        self.gemm(dz, self.transpose(Hd["w16"], Hd["cout"], Hd["k"]), dy, P, Hd["k"], Hd["cout"],
-                  Hd["cout"], Hd["cout"], Hd["k"])
+        self.gemm_mn(dz, False, Hd["w16"], True, dy, P, Hd["k"], Hd["cout"], Hd["cout"], Hd["k"],
+                     Hd["k"])
+        L = self.layers[-1]
+        y, P = self.saved[-1][1], self.saved[-1][4]
+        dz = torch.empty(P, L["cout"], dtype=torch.bfloat16, device=self.dev)
+        _lib.check(lib.splat_nn_act_grad(_p(dy), _p(y), _p(dz), _p(L["gb"]), P, L["cout"], 1, s),
+                   "act_grad")
         for i in range(len(self.layers) - 1, -1, -1):
             L = self.layers[i]
             cols, y, h, ho, P = self.saved[i]
-            dz = torch.empty(P, L["cout"], dtype=torch.bfloat16, device=self.dev)
-            _lib.check(lib.splat_nn_act_grad(_p(dy), _p(y), _p(dz), _p(L["gb"]), P, L["cout"], 1, s),
-                       "act_grad")
-            self.gemm(self.transpose(dz, P, L["cout"]), self.transpose(cols, P, L["k"]), L["gw"],
-                      L["cout"], L["k"], P, P, P, L["k"])
+            self.gemm_mn(dz, True, cols, True, L["gw"], L["cout"], L["k"], P, L["cout"], L["k"],
+                         L["k"])
             if i == 0:
                 break
             dcols = torch.empty(P, L["k"], device=self.dev)
-            self.gemm(dz, self.transpose(L["w16"], L["cout"], L["k"]), dcols, P, L["k"], L["cout"],
-                      L["cout"], L["cout"], L["k"])
-            dy = torch.empty(B * h * h, L["cin"], device=self.dev)
-            _lib.check(lib.splat_nn_col2im3x3(_p(dcols), _p(dy), B, h, h, L["cin"], 2, L["k"], s),
-                       "col2im3x3")
+            self.gemm_mn(dz, False, L["w16"], True, dcols, P, L["k"], L["cout"], L["cout"], L["k"],
+                         L["k"])
+            # col2im through the previous layer's ReLU: that layer's dz
+            prev = self.layers[i - 1]
+            dz = torch.empty(B * h * h, L["cin"], dtype=torch.bfloat16, device=self.dev)
+            _lib.check(lib.splat_nn_col2im_act3x3(_p(dcols), _p(self.saved[i - 1][1]), _p(dz),
+                                                  _p(prev["gb"]), B, h, h, L["cin"], 2, L["k"], s),
+                       "col2im_act3x3")
 
     def adam(self, lr: float):
         self.step_count += 1
-        s = self._s()
-        for prm in self.layers + [self.head]:
-            _lib.check(self.lib.splat_nn_adam(_p(prm["w"]), _p(prm["mw"]), _p(prm["vw"]),
-                                              _p(prm["gw"]), _p(prm["w16"]), prm["w"].numel(), lr,
-                                              self.step_count, s), "adam")
-            _lib.check(self.lib.splat_nn_adam(_p(prm["b"]), _p(prm["mb"]), _p(prm["vb"]),
-                                              _p(prm["gb"]), None, prm["b"].numel(), lr,
-                                              self.step_count, s), "adam")
+        _lib.check(self.lib.splat_nn_adam_multi(self._adam_segs, len(self._adam_segs), lr,
+                                                self.step_count, self._s()), "adam_multi")
 
     def check(self):
         torch.cuda.synchronize(self.dev)

@@ -93,7 +93,8 @@ def test_ctypes_signatures_match_header():
 
 @pytest.mark.parametrize("c_name,py_name", [("splat_params", "SplatParams"),
                                              ("splat_view", "SplatView"),
-                                             ("splat_batch", "SplatBatch")])
+                                             ("splat_batch", "SplatBatch"),
+                                             ("splat_adam_seg", "SplatAdamSeg")])
 def test_struct_layout_matches_header(tmp_path, c_name, py_name):
     """Size, and offset and size of every field, of the ctypes mirror against
     the C compiler's layout of the header's struct."""

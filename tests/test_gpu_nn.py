@@ -1,6 +1,7 @@
 """The warm-start network's convolutions (im2col + tcgen05 GEMM, bias/ReLU,
 col2im): one layer's forward and gradients against an fp64 CPU computation on
-the same bf16 operands, the whole network against torch's fp32 conv2d, a
+the same bf16 operands, the fused col2im + ReLU gradient and the one-launch
+Adam against their unfused forms, the whole network against torch's fp32 conv2d, a
 short training run that lowers the loss, and the learned warm start's gain
 over plain fitting and over its image-blind ablation."""
 
@@ -82,6 +83,37 @@ def _col2im(dcols, shape, stride=2):
     return dxp[:, 1:-1, 1:-1]
 
 
+@pytest.mark.parametrize("n,h,w,c,st", [(2, 20, 20, 3, 2), (1, 33, 17, 12, 2), (2, 16, 16, 8, 1),
+                                         (1, 5, 2800, 3, 2), (3, 9, 9, 32, 2),
+                                         (1, 12, 10, 64, 2), (2, 8, 8, 128, 2)])
+def test_im2col_paths_match_numpy(n, h, w, c, st):
+    """Every im2col path -- shared-memory row staging (few channels), the
+    one-element-per-lane gather (rows wider than the staging), 16-byte
+    channel vectors (C a multiple of 8) -- bit-exact against numpy, the
+    columns past 9C zero."""
+    import ctypes as C
+
+    import torch
+
+    from jaxsplat_gb300 import _lib
+
+    lib = _lib.load()
+    kp = (9 * c + 7) // 8 * 8
+    ho, wo = (h - 1) // st + 1, (w - 1) // st + 1
+    g = torch.Generator(device="cuda").manual_seed(n * h + w + c)
+    x = torch.randn(n, h, w, c, device="cuda", generator=g).bfloat16()
+    cols = torch.full((n * ho * wo, kp), float("nan"), device="cuda", dtype=torch.bfloat16)
+    _lib.check(lib.splat_nn_im2col3x3(C.c_void_p(x.data_ptr()), C.c_void_p(cols.data_ptr()), n, h,
+                                      w, c, st, kp,
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "im2col")
+    torch.cuda.synchronize()
+    got = cols.float().cpu().numpy().astype(np.float64)
+    ref = _im2col(x.float().cpu().numpy().astype(np.float64), stride=st)
+    np.testing.assert_array_equal(got[:, :9 * c], ref)
+    assert not got[:, 9 * c:].any()
+
+
 def test_conv_layer_matches_fp64_cpu():
     """Layer 2 of the encoder (32 -> 64 channels, 3x3 stride 2) on the GPU --
     im2col, tcgen05 GEMM, bias + ReLU, and in the backward the ReLU mask,
@@ -118,9 +150,11 @@ def test_conv_layer_matches_fp64_cpu():
     gb = torch.zeros(cout, device="cuda")
     _lib.check(lib.splat_nn_act_grad(p(dy), p(y), p(dz), p(gb), P, cout, 1, s), "act_grad")
     gw = torch.empty(cout, kp, device="cuda")
-    net.gemm(net.transpose(dz, P, cout), net.transpose(cols, P, kp), gw, cout, kp, P, P, P, kp)
+    # the network's own calls: both operands pixel-major (MN-major) for the
+    # weight gradient, the weights as stored (MN-major B) for the data gradient
+    net.gemm_mn(dz, True, cols, True, gw, cout, kp, P, cout, kp, kp)
     dcols = torch.empty(P, kp, device="cuda")
-    net.gemm(dz, net.transpose(L["w16"], cout, kp), dcols, P, kp, cout, cout, cout, kp)
+    net.gemm_mn(dz, False, L["w16"], True, dcols, P, kp, cout, cout, kp, kp)
     dx = torch.empty(n, h, h, cin, device="cuda")
     _lib.check(lib.splat_nn_col2im3x3(p(dcols), p(dx), n, h, h, cin, 2, kp, s), "col2im")
     torch.cuda.synchronize()
@@ -147,6 +181,82 @@ def test_conv_layer_matches_fp64_cpu():
     assert rel(f64(gw)[:, :9 * cin], dz64.T @ cols_ref) <= 1e-5
     assert not f64(gw)[:, 9 * cin:].any()
     assert rel(f64(dx), _col2im(dz64 @ W, (n, h, h, cin))) <= 1e-5
+
+
+def test_col2im_act_matches_col2im_then_act_grad():
+    """The fused gather through the previous layer's ReLU (the network's
+    backward) against col2im followed by act_grad: dz bit-identical, the
+    channel sums within fp32 summation-order noise."""
+    import ctypes as C
+
+    import torch
+
+    from jaxsplat_gb300 import _lib
+
+    lib = _lib.load()
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    g = torch.Generator(device="cuda").manual_seed(4)
+    # stride 2 takes the quad kernel, stride 1 and 12 channels the row kernel
+    for n, h, cin, st in [(2, 64, 32, 2), (3, 33, 64, 2), (1, 16, 128, 2), (2, 20, 32, 1),
+                          (2, 18, 12, 2)]:
+        kp = 9 * cin
+        ho = (h - 1) // st + 1
+        P = n * ho * ho
+        dcols = torch.randn(P, kp, device="cuda", generator=g)
+        y = torch.randn(n * h * h, cin, device="cuda", generator=g).bfloat16()
+        dx = torch.empty(n, h, h, cin, device="cuda")
+        _lib.check(lib.splat_nn_col2im3x3(p(dcols), p(dx), n, h, h, cin, st, kp, s), "col2im")
+        dz_ref = torch.empty(n * h * h, cin, dtype=torch.bfloat16, device="cuda")
+        gb_ref = torch.zeros(cin, device="cuda")
+        _lib.check(lib.splat_nn_act_grad(p(dx), p(y), p(dz_ref), p(gb_ref), n * h * h, cin, 1, s),
+                   "act_grad")
+        dz = torch.empty_like(dz_ref)
+        gb = torch.zeros(cin, device="cuda")
+        _lib.check(lib.splat_nn_col2im_act3x3(p(dcols), p(y), p(dz), p(gb), n, h, h, cin, st, kp,
+                                              s), "col2im_act3x3")
+        torch.cuda.synchronize()
+        assert torch.equal(dz.view(torch.int16), dz_ref.view(torch.int16)), (n, h, cin, st)
+        assert _rel(gb, gb_ref) < 1e-5, (n, h, cin, st)
+
+
+def test_adam_multi_matches_per_array_adam():
+    """One Adam launch over several arrays (with and without bf16 copies)
+    against one launch per array: bit-identical."""
+    import ctypes as C
+
+    import torch
+
+    from jaxsplat_gb300 import _lib
+
+    lib = _lib.load()
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    g = torch.Generator(device="cuda").manual_seed(6)
+    sizes = [288 * 64, 64, 0, 1000, 224 * 256, 7]
+    arrays = [[torch.randn(n, device="cuda", generator=g) for _ in range(4)] for n in sizes]
+    for arr in arrays:
+        arr[2].abs_()  # second moments are non-negative
+    a16 = [torch.zeros(n, dtype=torch.bfloat16, device="cuda") if k % 2 == 0 else None
+           for k, n in enumerate(sizes)]
+    ref = [[t.clone() for t in arr[:3]] for arr in arrays]
+    ref16 = [t.clone() if t is not None else None for t in a16]
+    for step in (1, 2, 3):
+        for (w, m, v), (_, _, _, gr), w16 in zip(ref, arrays, ref16):
+            if w.numel() == 0:
+                continue
+            _lib.check(lib.splat_nn_adam(p(w), p(m), p(v), p(gr), p(w16) if w16 is not None else None,
+                                         w.numel(), 1e-3, step, s), "adam")
+        segs = (_lib.SplatAdamSeg * len(sizes))(*[
+            _lib.SplatAdamSeg(w.data_ptr(), m.data_ptr(), v.data_ptr(), gr.data_ptr(),
+                              w16.data_ptr() if w16 is not None else None, w.numel())
+            for (w, m, v, gr), w16 in zip(arrays, a16)])
+        _lib.check(lib.splat_nn_adam_multi(segs, len(sizes), 1e-3, step, s), "adam_multi")
+    torch.cuda.synchronize()
+    for (w, m, v, _), (rw, rm, rv), w16, r16 in zip(arrays, ref, a16, ref16):
+        assert torch.equal(w, rw) and torch.equal(m, rm) and torch.equal(v, rv)
+        if w16 is not None:
+            assert torch.equal(w16.view(torch.int16), r16.view(torch.int16))
 
 
 def test_training_lowers_the_loss():
