@@ -171,10 +171,10 @@ class OursStep:
         bw = sc.spec.block_width
         tiles = ((w + bw - 1) // bw) * ((h + bw - 1) // bw)
         tile_passes = radix_passes(max(1, (tiles - 1).bit_length()))
-        # project (+ packing), depth keys (+ digit counts), 4-pass depth sort
-        # (+ offsets), emission (offsets, expansion + digit counts), tile sort
-        # (+ offsets), bins, raster fwd (+ loss), raster bwd, project bwd
-        self.kernels_per_step = 1 + 1 + 5 + 2 + (1 + tile_passes) + 1 + 1 + 1 + 1
+        # project (+ packing), depth keys (+ digit counts), 4-pass depth sort,
+        # emission (offsets, expansion + digit counts), tile sort, bins,
+        # raster fwd (+ loss), raster bwd, project bwd
+        self.kernels_per_step = 1 + 1 + 4 + 2 + tile_passes + 1 + 1 + 1 + 1
         self.passes = tile_passes
 
     def launches_per_step(self):
@@ -307,11 +307,11 @@ class BatchStep:
             s.capture_io(self.host_in, self.host_out)
         b = s.batch
         tile_passes = radix_passes(max(1, (int(b.num_tiles) - 1).bit_length()))
-        # project, depth keys (+ digit counts), 4-pass depth sort (+ offsets),
-        # emission (2, + digit counts), tile sort (+ offsets), bins, tile
-        # costs, 3-pass cost sort (+hist, offsets), raster fwd (+ loss),
-        # raster bwd, project bwd; the projection writes the packed records
-        self.kernels_per_step = 1 + 1 + 5 + 2 + (1 + tile_passes) + 1 + 1 + 5 + 1 + 1 + 1
+        # project, depth keys (+ digit counts), 4-pass depth sort, emission
+        # (2, + digit counts), tile sort, bins, tile costs, 3-pass cost sort
+        # (+ hist), raster fwd (+ loss), raster bwd, project bwd; the
+        # projection writes the packed records
+        self.kernels_per_step = 1 + 1 + 4 + 2 + tile_passes + 1 + 1 + 4 + 1 + 1 + 1
         self.passes = tile_passes
 
     def launches_per_step(self):

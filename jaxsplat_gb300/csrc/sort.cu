@@ -82,22 +82,6 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(HistArgs a) {
     }
 }
 
-// Exclusive scan of each pass's 256 digit counts (one block per pass).
-__global__ void __launch_bounds__(kRadix) radix_offsets_kernel(const unsigned *hist, unsigned *offs) {
-    __shared__ unsigned s[kRadix];
-    const int d = blockIdx.x, t = threadIdx.x;
-    const unsigned x = hist[d * kRadix + t];
-    s[t] = x;
-    __syncthreads();
-    for (int o = 1; o < kRadix; o <<= 1) {
-        const unsigned y = t >= o ? s[t - o] : 0u;
-        __syncthreads();
-        s[t] += y;
-        __syncthreads();
-    }
-    offs[d * kRadix + t] = s[t] - x;
-}
-
 // Digit counts of the keys a producer kernel writes, for every pass of the
 // radix sort that follows (the sort then skips its histogram pass over the
 // keys): a block counts in shared memory and adds its nonzero counts to the
@@ -213,7 +197,7 @@ struct PassArgs {
     Count count;
     int shift;
     unsigned mask;
-    const unsigned *offs;  // [256] exclusive global digit offsets of this pass
+    const unsigned *hist;  // [256] global digit counts of this pass (complete before the pass)
     uint32_t *lookback;    // [nparts][256]
     unsigned *ticket;
     uint32_t *status;
@@ -224,6 +208,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     __shared__ unsigned s_whist[kSortWarps][kRadix];  // per-warp digit counts -> exclusive offsets
     __shared__ int s_delta[kRadix];                   // block-local digit start, then global - local
     __shared__ unsigned s_wsum[kSortWarps];
+    __shared__ unsigned s_hsum[kSortWarps];
     __shared__ uint32_t s_keys[kPartKeys];
     __shared__ int32_t s_vals[kPartKeys];
     __shared__ int s_part;
@@ -231,6 +216,10 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) s_part = (int)atomicAdd(a.ticket, 1u);
     for (int i = lane; i < kRadix; i += 32) s_whist[warp][i] = 0u;
+    // this pass's global count of digit t: every block scans the 256 counts
+    // itself (their exclusive prefix is the digit's first output slot), so
+    // no separate offsets kernel runs between the producer and the pass
+    const unsigned hc = a.hist[t];
     __syncthreads();
     const int part = s_part;
     // counts are at most 2^30 - 1 (checked on the host), so 32-bit indices
@@ -287,19 +276,31 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     const unsigned cnt = run;
     uint32_t *my = a.lookback + (size_t)part * kRadix + t;
     publish_word(my, (part == 0 ? kLbPrefix : kLbAgg) | (cnt & kLbMask));
-    // block-local exclusive scan of the digit counts: warp scans + warp totals
-    unsigned incl = cnt;
+    // block-local exclusive scans of the digit counts (this partition's and
+    // the pass's global ones): warp scans + warp totals
+    unsigned incl = cnt, hincl = hc;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
+        const unsigned hy = __shfl_up_sync(0xffffffffu, hincl, o);
+        if (lane >= o) {
+            incl += y;
+            hincl += hy;
+        }
     }
-    if (lane == 31) s_wsum[warp] = incl;
+    if (lane == 31) {
+        s_wsum[warp] = incl;
+        s_hsum[warp] = hincl;
+    }
     __syncthreads();
-    unsigned wbase = 0;
+    unsigned wbase = 0, hbase = 0;
 #pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) wbase += w < warp ? s_wsum[w] : 0u;
+    for (int w = 0; w < kSortWarps; ++w) {
+        wbase += w < warp ? s_wsum[w] : 0u;
+        hbase += w < warp ? s_hsum[w] : 0u;
+    }
     const unsigned bstart = wbase + incl - cnt;
+    const unsigned goff = hbase + hincl - hc;  // first global slot of digit t
     s_delta[t] = (int)bstart;
     __syncthreads();
 
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     }
     __syncthreads();  // every thread has read s_delta for its staging
     // staged position i of digit d goes to global position i + delta[d]
-    s_delta[t] = (int)(a.offs[t] + excl) - (int)bstart;
+    s_delta[t] = (int)(goff + excl) - (int)bstart;
     __syncthreads();
     const int nvalid = min(count - part * kPartKeys, kPartKeys);
 #pragma unroll 4
@@ -344,7 +345,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
 struct RadixBufs {
     uint32_t *ka, *kb;
     int32_t *va, *vb;
-    unsigned *hist, *offs, *tickets;
+    unsigned *hist, *tickets;
     uint32_t *lookback;
     size_t zero_bytes;  // hist + tickets + lookback, contiguous from hist
     long long nparts;
@@ -359,7 +360,6 @@ static RadixBufs radix_layout(Arena &ar, long long count, int end_bit) {
     b.kb = ar.take<uint32_t>(count);
     b.va = ar.take<int32_t>(count);
     b.vb = ar.take<int32_t>(count);
-    b.offs = ar.take<unsigned>((size_t)kMaxPasses * kRadix);
     const size_t before = (ar.used + 255) & ~size_t(255);
     b.hist = ar.take<unsigned>((size_t)kMaxPasses * kRadix);
     b.tickets = ar.take<unsigned>(kMaxPasses);
@@ -402,8 +402,6 @@ static int radix_sort(uint32_t *status, uint32_t spin, const RadixBufs &b, Count
         radix_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(h);
         if (int rc = check_launch("radix_hist_kernel")) return rc;
     }
-    radix_offsets_kernel<<<b.passes, kRadix, 0, s>>>(b.hist, b.offs);
-    if (int rc = check_launch("radix_offsets_kernel")) return rc;
     uint32_t *kin = b.ka, *kout = b.kb;
     int32_t *vin = b.va, *vout = b.vb;
     for (int d = 0; d < b.passes; ++d) {
@@ -416,7 +414,7 @@ static int radix_sort(uint32_t *status, uint32_t spin, const RadixBufs &b, Count
         pa.count = count;
         pa.shift = d * kRadixBits;
         pa.mask = (1u << min(kRadixBits, end_bit - d * kRadixBits)) - 1u;
-        pa.offs = b.offs + d * kRadix;
+        pa.hist = b.hist + d * kRadix;
         pa.lookback = b.lookback + (size_t)d * b.nparts * kRadix;
         pa.ticket = b.tickets + d;
         pa.status = status;
