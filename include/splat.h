@@ -95,7 +95,9 @@ SPLAT_API int splat_version(void);
  *   means3d (N,3) scales (N,3) quats (N,4, w-x-y-z) viewmat (4,4)
  *   -> cov3d (N,6) xys (N,2) depths (N,1) radii (N,1) int32 conics (N,3)
  *      compensation (N,1) num_tiles_hit (N,1) int32 cum_tiles_hit (N,1) int32
- * total_out (optional, device int64): I as a 64-bit count. */
+ * total_out (optional, device int64): I as a 64-bit count.  cum_tiles_hit
+ * may be NULL when total_out is given: then only the total is produced
+ * (no scan). */
 SPLAT_API size_t splat_project_fwd_workspace_size(const splat_params *p);
 SPLAT_API int splat_project_fwd(const splat_params *p, const float *means3d, const float *scales,
                       const float *quats, const float *viewmat, float *cov3d, float *xys,

@@ -247,7 +247,10 @@ static int project_fwd_entry(const splat_params *p, const float *means3d, const 
     }
     NEED(means3d); NEED(scales); NEED(quats); NEED(viewmat); NEED(cov3d); NEED(xys);
     NEED(depths); NEED(radii); NEED(conics); NEED(compensation); NEED(num_tiles_hit);
-    if (!packed) NEED(cum_tiles_hit);  // optional only with the packed records
+    // without cum_tiles_hit only the intersection total is produced (the
+    // count-only kernel), so the total then has somewhere to go
+    if (!cum_tiles_hit && !total_out)
+        return fail(SPLAT_ERR_INVALID_ARG, "project_fwd needs cum_tiles_hit or total_out");
     NEED_WS(workspace);
     if (workspace_bytes < project_ws_bytes(*p))
         return fail(SPLAT_ERR_WORKSPACE, "project workspace too small: need %zu, got %zu",

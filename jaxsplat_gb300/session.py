@@ -138,7 +138,7 @@ class RenderSession(StreamingSteps):
 
     def measure_capacity(self, headroom: float = 1.25) -> int:
         """One projection with a host read of the count; sizes the buffers."""
-        self._project()
+        self._project(cum=True)
         torch.cuda.synchronize(self.dev)
         count = int(self.total.item())
         self._size(int(math.ceil(count * headroom)) + 4096)
@@ -155,7 +155,9 @@ class RenderSession(StreamingSteps):
     def _check(self, rc, what):
         _lib.check(rc, what)
 
-    def _project(self, pack=False):
+    def _project(self, pack=False, cum=False):
+        """The projection; the step reads only the intersection total, so
+        cum_tiles_hit is written only when asked (the sizing pass)."""
         P, pr = self._p, C.byref(self.params)
         if pack:  # the packed records too (no separate packing pass), and only the
             # intersection count: the step never reads cum_tiles_hit
@@ -169,8 +171,8 @@ class RenderSession(StreamingSteps):
         self._check(self.lib.splat_project_fwd(
             pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat), P(self.cov3d),
             P(self.xys), P(self.depths), P(self.radii), P(self.conics), P(self.comp),
-            P(self.ntiles), P(self.cum), P(self.total), P(self.proj_ws), self.proj_ws.numel(),
-            self._stream()), "project_fwd")
+            P(self.ntiles), P(self.cum) if cum else None, P(self.total), P(self.proj_ws),
+            self.proj_ws.numel(), self._stream()), "project_fwd")
 
     def step(self, mark=None, side=None):
         """Enqueue one forward+backward on the current stream (no host sync).

@@ -186,6 +186,17 @@ def test_misaligned_workspace_rejected_without_gpu(lib):
     assert rc == 1 and b"256-byte aligned" in lib.splat_last_error()
 
 
+def test_project_fwd_needs_a_count_output_without_gpu(lib):
+    """cum_tiles_hit is optional when total_out is given (count-only
+    projection); with neither the call is refused before any CUDA call."""
+    from jaxsplat_gb300 import _lib
+
+    p = _lib.make_params(10, (32, 32), (32.0, 32.0), (16.0, 16.0), 1.0, 0.01, 16)
+    fake = [C.c_void_p(0x10000 + 256 * i) for i in range(11)]
+    rc = lib.splat_project_fwd(C.byref(p), *fake, None, None, C.c_void_p(0x20000), 1 << 20, None)
+    assert rc == 1 and b"cum_tiles_hit or total_out" in lib.splat_last_error()
+
+
 def test_misaligned_tile_bins_rejected_without_gpu(lib):
     """tile_bins is accessed as int2: a 4-byte offset is refused before any
     CUDA call."""
