@@ -228,7 +228,8 @@ SPLAT_API int splat_rasterize_bwd(const splat_params *p, int64_t num_intersects,
 /* ---------------------------------------------------------------------- */
 /* Projection backward.  Replaces ops::project::bwd::xla (lib/ops.cu:63-105,
  * kernel lib/kernels/backward.cu:345-418).  Outputs are overwritten.
- *   -> v_mean3d (N,3) v_scale (N,3) v_quat (N,4) v_cov2d (N,3) v_cov3d (N,6) */
+ *   -> v_mean3d (N,3) v_scale (N,3) v_quat (N,4) v_cov2d (N,3) v_cov3d (N,6)
+ * v_cov2d and v_cov3d (intermediate cotangents) may be NULL: not written. */
 SPLAT_API int splat_project_bwd(const splat_params *p, const float *means3d, const float *scales,
                       const float *quats, const float *viewmat, const float *cov3d,
                       const int32_t *radii, const float *conics, const float *compensation,

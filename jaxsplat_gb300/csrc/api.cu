@@ -456,8 +456,7 @@ int splat_project_bwd(const splat_params *p, const float *means3d, const float *
     if (p->num_points == 0) return SPLAT_OK;
     NEED(means3d); NEED(scales); NEED(quats); NEED(viewmat); NEED(cov3d); NEED(radii);
     NEED(conics); NEED(compensation); NEED(v_xy); NEED(v_depth); NEED(v_conic);
-    NEED(v_compensation); NEED(v_mean3d); NEED(v_scale); NEED(v_quat); NEED(v_cov2d);
-    NEED(v_cov3d);
+    NEED(v_compensation); NEED(v_mean3d); NEED(v_scale); NEED(v_quat);  // v_cov2d, v_cov3d optional
     return launch_project_bwd(*p, means3d, scales, quats, viewmat, cov3d, radii, conics,
                               compensation, v_xy, v_depth, v_conic, v_compensation, v_mean3d,
                               v_scale, v_quat, v_cov2d, v_cov3d, (cudaStream_t)stream);

@@ -193,6 +193,7 @@ struct ProjBwdArgs {
     float *v_mean3d, *v_scale, *v_quat, *v_cov2d, *v_cov3d;
 };
 
+// One Gaussian per thread; v_cov2d and v_cov3d only when asked for.
 __global__ void __launch_bounds__(256) project_bwd_kernel(ProjBwdArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -208,12 +209,17 @@ __global__ void __launch_bounds__(256) project_bwd_kernel(ProjBwdArgs a) {
     for (int k = 0; k < 3; ++k) {
         a.v_mean3d[3 * i + k] = g.vmean[k];
         a.v_scale[3 * i + k] = g.vscale[k];
-        a.v_cov2d[3 * i + k] = g.vc2[k];
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) a.v_quat[4 * i + k] = g.vquat[k];
+    if (a.v_cov2d) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) a.v_cov3d[6 * i + k] = g.vc3[k];
+        for (int k = 0; k < 3; ++k) a.v_cov2d[3 * i + k] = g.vc2[k];
+    }
+    if (a.v_cov3d) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.v_cov3d[6 * i + k] = g.vc3[k];
+    }
 }
 
 // ---------------------------------------------------------------------------

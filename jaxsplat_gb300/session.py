@@ -74,7 +74,6 @@ class RenderSession(StreamingSteps):
             setattr(self, name, t)
         self.v_xy, self.v_conic = E(n, 2, **f32), E(n, 3, **f32)
         self.zeros_n1 = torch.zeros(n, 1, **f32)
-        self.v_cov2d, self.v_cov3d = E(n, 3, **f32), E(n, 6, **f32)
         self.capacity = None
         self.graph = None
         self.graph_io = None
@@ -222,7 +221,7 @@ class RenderSession(StreamingSteps):
             pr, P(self.means3d), P(self.scales), P(self.quats), P(self.viewmat), P(self.cov3d),
             P(self.radii), P(self.conics), P(self.comp), P(self.v_xy), P(self.zeros_n1),
             P(self.v_conic), P(self.zeros_n1), P(self.v_mean3d), P(self.v_scale),
-            P(self.v_quat), P(self.v_cov2d), P(self.v_cov3d), s), "project_bwd")
+            P(self.v_quat), None, None, s), "project_bwd")  # the cov cotangents are not returned
         mark("end")
 
     def count_pairs(self):
