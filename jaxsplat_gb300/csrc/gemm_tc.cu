@@ -108,20 +108,21 @@ __host__ __device__ constexpr uint32_t mma_idesc(int m, int n, bool a_mn = false
            ((b_mn ? 1u : 0u) << 16) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-// Polls (non-blocking test_wait) with a short sleep between polls; gives up
-// after `limit` polls (about limit x 0.1 us).
+// Waits for the barrier's phase with mbarrier.try_wait, which suspends the
+// thread until the phase completes or a time limit (the hint, ~1 us) passes;
+// gives up after `limit` tries.  (Polling test_wait with a sleep between
+// polls wakes up to one sleep late at every ring stage.)
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
     for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(bar), "r"(parity)
+            : "r"(bar), "r"(parity), "r"(1000u)
             : "memory");
         if (done) return true;
-        if (i > 64) __nanosleep(100);
     }
     return false;
 }
@@ -648,7 +649,7 @@ static int gemm_f32(const void *A, bool a_mn, const void *B, bool b_mn, float *C
     g.accumulate = accumulate;
     g.mode = kOutF32;
     g.status = status_dev;
-    g.spin_limit = 1u << 21;  // ~0.2 s of polling per wait
+    g.spin_limit = 1u << 18;  // tries of up to ~1 us each per wait
     return run_gemm(A, B, g, lda, ldb, a_mn, b_mn, stream);
 }
 
@@ -683,7 +684,7 @@ int splat_gemm_bf16_bias_act(const void *A, const void *B, const float *bias, vo
     g.relu = relu;
     g.mode = y16 ? kOutBiasBF16 : kOutBiasF32;
     g.status = status_dev;
-    g.spin_limit = 1u << 21;
+    g.spin_limit = 1u << 18;
     return run_gemm(A, B, g, lda, ldb, false, false, (cudaStream_t)stream);
 }
 
