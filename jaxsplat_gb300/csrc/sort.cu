@@ -209,6 +209,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     __shared__ int s_delta[kRadix];                   // block-local digit start, then global - local
     __shared__ unsigned s_wsum[kSortWarps];
     __shared__ unsigned s_hsum[kSortWarps];
+    __shared__ unsigned s_hc[kRadix];  // this pass's global digit counts
     __shared__ uint32_t s_keys[kPartKeys];
     __shared__ int32_t s_vals[kPartKeys];
     __shared__ int s_part;
@@ -218,8 +219,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     for (int i = lane; i < kRadix; i += 32) s_whist[warp][i] = 0u;
     // this pass's global count of digit t: every block scans the 256 counts
     // itself (their exclusive prefix is the digit's first output slot), so
-    // no separate offsets kernel runs between the producer and the pass
-    const unsigned hc = a.hist[t];
+    // no separate offsets kernel runs between the producer and the pass.
+    // Parked in shared memory until the scan (no register across the ranking).
+    s_hc[t] = a.hist[t];
     __syncthreads();
     const int part = s_part;
     // counts are at most 2^30 - 1 (checked on the host), so 32-bit indices
@@ -276,31 +278,19 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
     const unsigned cnt = run;
     uint32_t *my = a.lookback + (size_t)part * kRadix + t;
     publish_word(my, (part == 0 ? kLbPrefix : kLbAgg) | (cnt & kLbMask));
-    // block-local exclusive scans of the digit counts (this partition's and
-    // the pass's global ones): warp scans + warp totals
-    unsigned incl = cnt, hincl = hc;
+    // block-local exclusive scan of the digit counts: warp scans + warp totals
+    unsigned incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-        const unsigned hy = __shfl_up_sync(0xffffffffu, hincl, o);
-        if (lane >= o) {
-            incl += y;
-            hincl += hy;
-        }
+        if (lane >= o) incl += y;
     }
-    if (lane == 31) {
-        s_wsum[warp] = incl;
-        s_hsum[warp] = hincl;
-    }
+    if (lane == 31) s_wsum[warp] = incl;
     __syncthreads();
-    unsigned wbase = 0, hbase = 0;
+    unsigned wbase = 0;
 #pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-        wbase += w < warp ? s_wsum[w] : 0u;
-        hbase += w < warp ? s_hsum[w] : 0u;
-    }
+    for (int w = 0; w < kSortWarps; ++w) wbase += w < warp ? s_wsum[w] : 0u;
     const unsigned bstart = wbase + incl - cnt;
-    const unsigned goff = hbase + hincl - hc;  // first global slot of digit t
     s_delta[t] = (int)bstart;
     __syncthreads();
 
@@ -324,7 +314,20 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_kernel(PassArgs a) {
         excl = lookback_digit(a.lookback + t, kRadix, part, a.spin_limit, a.status);
         publish_word(my, kLbPrefix | ((excl + cnt) & kLbMask));
     }
-    __syncthreads();  // every thread has read s_delta for its staging
+    // the pass's global digit offsets: exclusive scan of its digit counts
+    const unsigned hc = s_hc[t];
+    unsigned hincl = hc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned hy = __shfl_up_sync(0xffffffffu, hincl, o);
+        if (lane >= o) hincl += hy;
+    }
+    if (lane == 31) s_hsum[warp] = hincl;
+    __syncthreads();  // every thread has read s_delta for its staging; s_hsum is complete
+    unsigned hbase = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) hbase += w < warp ? s_hsum[w] : 0u;
+    const unsigned goff = hbase + hincl - hc;  // first global slot of digit t
     // staged position i of digit d goes to global position i + delta[d]
     s_delta[t] = (int)(goff + excl) - (int)bstart;
     __syncthreads();
