@@ -519,7 +519,6 @@ SPLAT_API int splat_gemm_bf16_bias_act(const void *A, const void *B, const float
  *   bias_act:  y = act(acc + bias) (ReLU when relu != 0), rows x cols, to y
  *     (bf16) and/or y32 (fp32)
  *   act_grad:  dz = dy * [y > 0] (or dy) as bf16; dbias += column sums
- *   transpose_bf16: out[c*ld_out + r] = in[r*cols + c]
  *   adam: w -= lr mhat / (sqrt(vhat) + 1e-8) (b1 0.9, b2 0.999, step >= 1),
  *     w16 (optional) = bf16(w) */
 SPLAT_API int splat_nn_im2col3x3(const void *x, void *cols, int n, int h, int w, int c, int stride,
@@ -533,8 +532,6 @@ SPLAT_API int splat_nn_bias_act(const float *acc, const float *bias, void *y, fl
                                 int64_t rows, int cols, int relu, splat_stream_t stream);
 SPLAT_API int splat_nn_act_grad(const float *dy, const void *y, void *dz, float *dbias,
                                 int64_t rows, int cols, int relu, splat_stream_t stream);
-SPLAT_API int splat_nn_transpose_bf16(const void *in, void *out, int64_t rows, int cols,
-                                      int64_t ld_out, splat_stream_t stream);
 SPLAT_API int splat_nn_adam(float *w, float *m, float *v, const float *g, void *w16, int64_t n,
                             float lr, int step, splat_stream_t stream);
 /* Adam over up to 16 parameter arrays in one launch (each as splat_nn_adam;

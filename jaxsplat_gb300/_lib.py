@@ -134,7 +134,6 @@ _SIGS = [
     ("splat_nn_col2im_act3x3", C.c_int, [_v, _v, _v, _v] + [C.c_int] * 6 + [_v]),
     ("splat_nn_bias_act", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),
     ("splat_nn_act_grad", C.c_int, [_v, _v, _v, _v, C.c_int64, C.c_int, C.c_int, _v]),
-    ("splat_nn_transpose_bf16", C.c_int, [_v, _v, C.c_int64, C.c_int, C.c_int64, _v]),
     ("splat_nn_adam", C.c_int, [_v, _v, _v, _v, _v, C.c_int64, C.c_float, C.c_int, _v]),
     ("splat_nn_adam_multi", C.c_int, [C.POINTER(SplatAdamSeg), C.c_int, C.c_float, C.c_int, _v]),
 ]

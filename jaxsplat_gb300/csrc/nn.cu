@@ -1,7 +1,7 @@
 // nn.cu -- the warm-start network's non-GEMM kernels: 3x3 convolutions as
 // im2col + tensor-core GEMM (gemm_tc.cu), so this file holds the gathers
 // around the GEMM (im2col, col2im), the bias/ReLU epilogue and its gradient,
-// operand transposes and the Adam update.  Activations are NHWC bf16,
+// and the Adam update.  Activations are NHWC bf16,
 // gradients fp32, weights fp32 masters with bf16 copies for the GEMMs.
 #include <cuda_bf16.h>
 
@@ -403,25 +403,6 @@ __global__ void act_grad_kernel(const float *__restrict__ dy, const __nv_bfloat1
         if (s_db[j] != 0.f) atomicAdd(&dbias[j], s_db[j]);
 }
 
-// out[c, r] = in[r, c] for a rows x cols bf16 matrix (32x32 tiles).
-__global__ void transpose_bf16_kernel(const __nv_bfloat16 *in, __nv_bfloat16 *out, long long rows,
-                                      int cols, long long ld_out) {
-    __shared__ __nv_bfloat16 tile[32][33];
-    const long long r0 = (long long)blockIdx.y * 32;
-    const int c0 = blockIdx.x * 32;
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        const long long r = r0 + k;
-        const int c = c0 + threadIdx.x;
-        tile[k][threadIdx.x] = (r < rows && c < cols) ? in[r * cols + c] : __float2bfloat16(0.f);
-    }
-    __syncthreads();
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        const int c = c0 + k;
-        const long long r = r0 + threadIdx.x;
-        if (c < cols && r < rows) out[(long long)c * ld_out + r] = tile[threadIdx.x][k];
-    }
-}
-
 // Adam (b1 0.9, b2 0.999, eps 1e-8) on fp32 masters; refreshes bf16 copies.
 __global__ void adam_kernel(float *w, float *m, float *v, const float *g, __nv_bfloat16 *w16,
                             long long n, float lr, float c1, float c2) {
@@ -591,18 +572,6 @@ int splat_nn_act_grad(const float *dy, const void *y, void *dz, float *dbias, in
         dy, static_cast<const __nv_bfloat16 *>(y), static_cast<__nv_bfloat16 *>(dz), dbias, rows,
         cols, relu);
     return check_launch("act_grad_kernel");
-}
-
-int splat_nn_transpose_bf16(const void *in, void *out, int64_t rows, int cols, int64_t ld_out,
-                            splat_stream_t stream) {
-    if (!in || !out || rows < 0 || cols <= 0 || ld_out < rows)
-        return fail(SPLAT_ERR_INVALID_ARG, "transpose_bf16: bad arguments");
-    dim3 grid((cols + 31) / 32, (unsigned)((rows + 31) / 32));
-    if (grid.y > 65535) return fail(SPLAT_ERR_INVALID_ARG, "transpose_bf16: too many rows");
-    transpose_bf16_kernel<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>(
-        static_cast<const __nv_bfloat16 *>(in), static_cast<__nv_bfloat16 *>(out), rows, cols,
-        ld_out);
-    return check_launch("transpose_bf16_kernel");
 }
 
 int splat_nn_adam(float *w, float *m, float *v, const float *g, void *w16, int64_t n, float lr,

@@ -124,12 +124,6 @@ class ConvNet:
             M, N, K, K, K, N, int(relu), _p(self.status), self._s()), "gemm_bf16_bias_act")
         return y
 
-    def transpose(self, x, rows, cols):
-        out = torch.empty(cols, rows, dtype=torch.bfloat16, device=self.dev)
-        _lib.check(self.lib.splat_nn_transpose_bf16(_p(x), _p(out), rows, cols, rows, self._s()),
-                   "transpose_bf16")
-        return out
-
     # -- forward / backward ------------------------------------------------------
     def forward(self, x):
         """x: (B, 512, 512, 3) bf16 NHWC -> (B*32*32, 224) fp32."""
