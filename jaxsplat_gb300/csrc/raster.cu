@@ -602,30 +602,42 @@ __global__ void __launch_bounds__(kMaxTile) raster_fwd_kernel(RasterFwdArgs a) {
 // ---------------------------------------------------------------------------
 // Backward.
 
-// Sum of 8 values over the warp, transposed: on return lane L holds the
-// warp total of value (L >> 2) & 7.  `lane` is the caller's lane index (the
-// pixel layout decides it, not threadIdx.x).
-__device__ __forceinline__ float warp_sum8_transposed(const float v[8], int lane) {
-    float b[4], c[2];
+// Sums over the warp of 8 values, transposed, and of one more value `op`:
+// on return lane L holds the warp total of value (L >> 2) & 7, and *op_total
+// the total of op in every lane.  Each step exchanges half of what a lane
+// holds with the lane 16, 8, then 4 apart (keeping the other half), then
+// finishes with two full butterfly steps; op takes five butterfly steps.
+// The adds of independent values issue as paired fp32 instructions (FADD2:
+// each component rounded as the scalar add; every sum keeps its order).
+// `lane` is the caller's lane index (the pixel layout decides it, not
+// threadIdx.x).
+__device__ __forceinline__ float warp_sum9_transposed(const float v[8], float op, int lane,
+                                                      float *op_total) {
     const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float send = u16 ? v[k] : v[k + 4];
-        const float keep = u16 ? v[k + 4] : v[k];
-        b[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
+    float2 b[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-        const float send = u8 ? b[k] : b[k + 2];
-        const float keep = u8 ? b[k + 2] : b[k];
-        c[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        const float s0 = u16 ? v[2 * k] : v[2 * k + 4], s1 = u16 ? v[2 * k + 1] : v[2 * k + 5];
+        const float k0 = u16 ? v[2 * k + 4] : v[2 * k], k1 = u16 ? v[2 * k + 5] : v[2 * k + 1];
+        b[k] = __fadd2_rn(make_float2(k0, k1), make_float2(__shfl_xor_sync(0xffffffffu, s0, 16),
+                                                           __shfl_xor_sync(0xffffffffu, s1, 16)));
     }
-    const float send = u4 ? c[0] : c[1];
-    const float keep = u4 ? c[1] : c[0];
-    float d = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    d += __shfl_xor_sync(0xffffffffu, d, 2);
-    d += __shfl_xor_sync(0xffffffffu, d, 1);
-    return d;
+    // b[0] = fields (0,1) or (4,5), b[1] = (2,3) or (6,7): step 2 keeps one pair
+    const float2 sendp = u8 ? b[0] : b[1], keepp = u8 ? b[1] : b[0];
+    const float2 c = __fadd2_rn(keepp, make_float2(__shfl_xor_sync(0xffffffffu, sendp.x, 8),
+                                                   __shfl_xor_sync(0xffffffffu, sendp.y, 8)));
+    const float send = u4 ? c.x : c.y;
+    const float keep = u4 ? c.y : c.x;
+    float o = op + __shfl_xor_sync(0xffffffffu, op, 16);
+    o += __shfl_xor_sync(0xffffffffu, o, 8);
+    o += __shfl_xor_sync(0xffffffffu, o, 4);
+    float2 e = make_float2(keep + __shfl_xor_sync(0xffffffffu, send, 4), o);
+    e = __fadd2_rn(e, make_float2(__shfl_xor_sync(0xffffffffu, e.x, 2),
+                                  __shfl_xor_sync(0xffffffffu, e.y, 2)));
+    e = __fadd2_rn(e, make_float2(__shfl_xor_sync(0xffffffffu, e.x, 1),
+                                  __shfl_xor_sync(0xffffffffu, e.y, 1)));
+    *op_total = e.y;
+    return e.x;
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -791,8 +803,8 @@ __device__ __forceinline__ void bwd_tile(const RasterBwdArgs &a, const TileCtx &
             const int g = s_gid[t];
             const int gc = kScene ? s_cidx[t] : g;
             if (wmask == 0xffffffffu && __popc(vmask) > kFewLanes) {
-                const float s8 = warp_sum8_transposed(g8, lane);
-                const float sop = warp_sum(g_op);
+                float sop;
+                const float s8 = warp_sum9_transposed(g8, g_op, lane, &sop);
                 if ((lane & 3) == 0) atomicAdd(grad_field(a, lane >> 2, g, gc), s8);
                 if (lane == 0) atomicAdd(&a.v_opac[gc], sop);
                 if (kAbs) {
@@ -1013,8 +1025,8 @@ __device__ __forceinline__ void bwd16_tile(const RasterBwdArgs &a, const TileCtx
             const int g = s_gid[t];
             const int gc = kScene ? s_cidx[t] : g;
             if (__popc(vmask) > kFewLanes) {
-                const float s8 = warp_sum8_transposed(g8, lane);
-                const float sop = warp_sum(g_op);
+                float sop;
+                const float s8 = warp_sum9_transposed(g8, g_op, lane, &sop);
                 if ((lane & 3) == 0) atomicAdd(grad_field(a, lane >> 2, g, gc), s8);
                 if (lane == 0) atomicAdd(&a.v_opac[gc], sop);
                 if (kAbs) {
