@@ -43,6 +43,28 @@ def random_init(num_points: int, seed: int = 0) -> dict:
                 opacities=opac)
 
 
+def random_init_device(num_points: int, seed: int, device) -> dict:
+    """random_init's distributions drawn on the device (torch's generator,
+    so not the same numbers as the numpy draw of the same seed): no host
+    work and no upload when a reused fitter restarts."""
+    g = torch.Generator(device=device).manual_seed(int(seed))
+    n = num_points
+    f32 = dict(dtype=torch.float32, device=device, generator=g)
+    lo = torch.tensor([-6.0, -6.0, -1.0], device=device)
+    hi = torch.tensor([6.0, 6.0, 1.0], device=device)
+    means = lo + (hi - lo) * torch.rand(n, 3, **f32)
+    scales = 0.5 * torch.rand(n, 3, **f32)
+    u, v, w = torch.rand(3, n, 1, **f32)
+    two_pi = 2.0 * math.pi
+    quats = torch.cat([torch.sqrt(1 - u) * torch.sin(two_pi * v),
+                       torch.sqrt(1 - u) * torch.cos(two_pi * v),
+                       torch.sqrt(u) * torch.sin(two_pi * w), torch.sqrt(u) * torch.cos(two_pi * w)],
+                      dim=1)
+    colors = torch.rand(n, 3, **f32)
+    opac = 0.5 + 0.5 * torch.rand(n, 1, **f32)
+    return dict(means3d=means, scales=scales, quats=quats, colors=colors, opacities=opac)
+
+
 def camera(img_shape):
     h, w = img_shape
     viewmat = np.eye(4, dtype=np.float32)
@@ -88,19 +110,28 @@ class Fitter:
 
     def reset(self, target=None, init: dict | None = None, seed: int = 0):
         """Start a new fit in the same buffers (the captured graph stays
-        valid): a new target and/or new raw parameters (random if not
-        given), Adam state cleared."""
+        valid): a new target and/or new raw parameters (host arrays or device
+        tensors; random, drawn on the device, if not given), Adam state
+        cleared."""
         s = self.sess
         if target is not None:
             t = target if isinstance(target, torch.Tensor) else torch.as_tensor(np.asarray(target, np.float32))
             s.target.copy_(t.reshape(s.target.shape))
         if init is None:
-            init = random_init(self.n, seed)
-        s.means3d.copy_(torch.as_tensor(np.asarray(init["means3d"], np.float32)).reshape(self.n, 3))
-        s.scales.copy_(torch.as_tensor(np.asarray(init["scales"], np.float32)).reshape(self.n, 3))
-        self.quats_raw.copy_(torch.as_tensor(np.asarray(init["quats"], np.float32)).reshape(self.n, 4))
-        self.colors_raw.copy_(torch.as_tensor(np.asarray(init["colors"], np.float32)).reshape(self.n, 3))
-        self.opac_raw.copy_(torch.as_tensor(np.asarray(init["opacities"], np.float32)).reshape(self.n, 1))
+            init = random_init_device(self.n, seed, s.dev)
+
+        def load(dst, x, cols):
+            # device tensors are copied on the device; host arrays uploaded
+            if isinstance(x, torch.Tensor):
+                dst.copy_(x.reshape(self.n, cols))
+            else:
+                dst.copy_(torch.as_tensor(np.asarray(x, np.float32)).reshape(self.n, cols))
+
+        load(s.means3d, init["means3d"], 3)
+        load(s.scales, init["scales"], 3)
+        load(self.quats_raw, init["quats"], 4)
+        load(self.colors_raw, init["colors"], 3)
+        load(self.opac_raw, init["opacities"], 1)
         self.m.zero_()
         self.v.zero_()
         self.step_count.zero_()

@@ -264,6 +264,26 @@ def from_grid(grid: np.ndarray) -> dict:
                 opacities=flat[:, 13:14].astype(np.float32))
 
 
+def from_grid_device(grid: torch.Tensor) -> dict:
+    """from_grid on the device in fp32 (grid: (32*32, 16*14) tensor): the
+    proposal goes from the network's output to the fitter's buffers without
+    a round trip through the host."""
+    fx, fy, cx, cy, tz = _cam()
+    g = grid.to(torch.float32).reshape(GRID, GRID, SLOTS, NPARAM)
+    idx = torch.arange(GRID, device=g.device, dtype=torch.float32)
+    gy, gx = torch.meshgrid(idx, idx, indexing="ij")
+    px = (gx[..., None] + 0.5 + g[..., 0]) * CELL
+    py = (gy[..., None] + 0.5 + g[..., 1]) * CELL
+    z = g[..., 2]
+    zc = z + tz
+    means = torch.stack([(px - cx) * zc / fx, (py - cy) * zc / fy, z], -1).reshape(-1, 3)
+    flat = g.reshape(-1, NPARAM)
+    q = flat[:, 6:10]
+    q = q / torch.clamp(torch.linalg.norm(q, dim=1, keepdim=True), min=1e-6)
+    return dict(means3d=means, scales=flat[:, 3:6].abs(), quats=q, colors=flat[:, 10:13],
+                opacities=flat[:, 13:14])
+
+
 # ---------------------------------------------------------------------------
 # Data, training, evaluation.
 
@@ -283,6 +303,7 @@ class WarmStart:
         self.net = ConvNet(device, seed)
         self.mu = np.zeros(SLOTS * NPARAM, np.float32)
         self.sd = np.ones(SLOTS * NPARAM, np.float32)
+        self._stats_dev = None
 
     def fit_normaliser(self, grids):
         """Per-parameter mean and spread over every slot of every set (numpy
@@ -299,6 +320,7 @@ class WarmStart:
         sd = (sq / n - mu * mu).clamp_min(0).sqrt() + 1e-3
         self.mu = np.tile(mu.cpu().numpy(), SLOTS).astype(np.float32)
         self.sd = np.tile(sd.cpu().numpy(), SLOTS).astype(np.float32)
+        self._stats_dev = None
 
     def _img(self, imgs):
         if isinstance(imgs, torch.Tensor):
@@ -347,18 +369,28 @@ class WarmStart:
         return hist
 
     def propose(self, image) -> dict:
-        """Initial raw parameters of 16384 Gaussians for a target image."""
-        out = self.net.forward(self._img(np.asarray(image)[None]))
-        grid = out.cpu().numpy() * self.sd + self.mu
-        return from_grid(grid)
+        """Initial raw parameters of 16384 Gaussians for a target image, as
+        device tensors (the network's output de-standardised and decoded on
+        the device)."""
+        img = image if isinstance(image, torch.Tensor) else np.asarray(image)
+        out = self.net.forward(self._img(img[None]))
+        mu, sd = self._stats()
+        return from_grid_device(out * sd + mu)
 
     def propose_mean(self, image=None) -> dict:
         """The ablation of ``propose``: the network's output forced to zero,
         i.e. the training sets' mean slot parameters in every cell of the
         grid -- the same grid layout and dataset statistics, nothing taken
         from the target image."""
-        grid = np.tile(self.mu, (GRID * GRID, 1))
-        return from_grid(grid)
+        mu, _ = self._stats()
+        return from_grid_device(mu.expand(GRID * GRID, -1))
+
+    def _stats(self):
+        """The standardisation (mean, std per slot parameter) on the device."""
+        if self._stats_dev is None:
+            self._stats_dev = (torch.as_tensor(np.asarray(self.mu, np.float32), device=self.dev),
+                               torch.as_tensor(np.asarray(self.sd, np.float32), device=self.dev))
+        return self._stats_dev
 
 
 def time_to_psnr(fitter: Fitter, target, seed: int = 0, psnr: float = 30.0,
@@ -376,8 +408,8 @@ def time_to_psnr(fitter: Fitter, target, seed: int = 0, psnr: float = 30.0,
     return reached, steps, time.perf_counter() - t0, p
 
 
-__all__ = ["ConvNet", "WarmStart", "to_grid", "from_grid", "fit_set", "time_to_psnr",
-           "random_init"]
+__all__ = ["ConvNet", "WarmStart", "to_grid", "from_grid", "from_grid_device", "fit_set",
+           "time_to_psnr", "random_init"]
 
 
 def make_dataset(n_sets: int, fit_steps: int, first_seed: int = 0, device="cuda", log=None,

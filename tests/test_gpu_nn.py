@@ -282,11 +282,11 @@ def test_learned_warm_start_beats_plain_fit():
     60 epochs) proposes initial Gaussians for 8 held-out targets; wall-clock
     to 30 dB PSNR (proposal, loading and fitting included) is compared with
     (a) the plain loop from random init: at most 0.25x (the target; measured
-    0.20x at this size on these seeds, 0.25x with 20 epochs, 0.21-0.23x on
-    their first four alone), and (b) the ablation that keeps
-    the proposal's grid layout and dataset-mean slot parameters but ignores
-    the image: at most 0.6x (measured ~0.26x), so the gain is what the network
-    reads in the image, not the fixed grid prior."""
+    0.19x at this size on these seeds with both starts made on the device),
+    and (b) the ablation that keeps the proposal's grid layout and
+    dataset-mean slot parameters but ignores the image: at most 0.6x
+    (measured ~0.24x), so the gain is what the network reads in the image,
+    not the fixed grid prior."""
     from jaxsplat_gb300.warmstart import run_experiment
 
     r = run_experiment(n_train=1000, fit_steps=300, epochs=60, lr=3e-3,
