@@ -21,11 +21,13 @@
 //  4. bin edges come from a binary search per tile.
 // Sorting uses an in-house onesweep LSD radix sort (Adinets & Merrill,
 // "Onesweep: A Faster Least Significant Digit Radix Sort for GPUs", 2022):
-// one histogram pass computes the digit counts of every pass; each pass is
-// one kernel in which a block takes a 4096-key partition by ticket, ranks its
-// keys stably with per-bit warp ballots and popc, publishes its per-digit counts, resolves
-// their global offsets by a decoupled look-back over preceding partitions and
-// scatters through shared memory.
+// the digit counts of every pass come from the kernel that writes the keys
+// (or one histogram pass); each pass is one kernel in which a block takes a
+// 4096-key partition by ticket, ranks its keys stably with per-bit warp
+// ballots and popc, publishes its per-digit counts, resolves their global
+// offsets by a decoupled look-back over preceding partitions (plus the
+// pass's digit starts, scanned from the counts by every block) and scatters
+// through shared memory.
 #include <algorithm>
 
 #include "splat_internal.cuh"
