@@ -651,8 +651,9 @@ enum { G_R, G_G, G_B, G_CA, G_CB, G_CC, G_X, G_Y, G_OP, G_AX, G_AY, G_FIELDS };
 
 // With at most this many contributing lanes a warp's lanes add their own
 // sums to the global gradients instead of reducing across the warp first
-// (swept 6-20 at 1920x1080: 16 fastest).
-constexpr int kFewLanes = 16;
+// (swept at 1920x1080: 12-14 fastest with the paired-add reduction, 16
+// before it; 20 is 4 % slower).
+constexpr int kFewLanes = 14;
 
 struct RasterBwdArgs {
     unsigned tiles_x, width, height, bw;
