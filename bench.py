@@ -54,7 +54,7 @@ L2_FLUSH_BYTES = 256 << 20
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # the dominant kernel on the 1M-Gaussian 1920x1080 scene, from one ncu
-# capture of that launch (104.39 MB read + 5.04 MB written).
+# capture of that launch (104.46 MB read + 4.77 MB written).
 NCU_TRAFFIC = {"raster_bwd": 104_461_312 + 4_772_352}
 # The batched backward captured at a quarter of the batch's Gaussian counts:
 # bytes read, bytes written, intersections.
