@@ -239,3 +239,39 @@ def test_xla_make_descriptor_rejects_bad_block_width(lib):
     with pytest.raises(_lib.SplatError):
         xla.make_descriptor(num_points=10, img_shape=(32, 32), f=(32.0, 32.0), c=(16.0, 16.0),
                             glob_scale=1.0, clip_thresh=0.01, block_width=0)
+
+
+def test_network_entry_points_reject_bad_arguments_without_gpu(lib):
+    """The warm-start network's entry points refuse bad shapes, strides,
+    alignments and segment tables before any CUDA call; the pointers are
+    placeholders that are never dereferenced."""
+    from jaxsplat_gb300 import _lib
+
+    a, b, c = C.c_void_p(0x10000), C.c_void_p(0x20000), C.c_void_p(0x30000)
+
+    def refused(rc, what):
+        assert rc == 1, what
+        assert what.encode() in lib.splat_last_error(), lib.splat_last_error()
+
+    # MN-major A stored [K, M]: its leading dimension must cover M
+    refused(lib.splat_gemm_bf16_mn(a, 1, b, 1, c, 48, 64, 64, 32, 64, 64, 0, None, None),
+            "covering the stored rows")
+    # K-major operands: K a multiple of 8
+    refused(lib.splat_gemm_bf16_mn(a, 0, b, 1, c, 64, 64, 60, 64, 64, 64, 0, None, None),
+            "multiples of 8")
+    # 16-byte aligned operands
+    refused(lib.splat_gemm_bf16(C.c_void_p(0x10008), b, c, 64, 64, 64, 64, 64, 64, 0, None,
+                                None), "16-byte aligned")
+    # im2col: kpad a multiple of 8 and >= 9c; cols 16-byte aligned
+    refused(lib.splat_nn_im2col3x3(a, b, 1, 8, 8, 3, 2, 28, None), "im2col3x3")
+    refused(lib.splat_nn_im2col3x3(a, C.c_void_p(0x20008), 1, 8, 8, 3, 2, 32, None),
+            "im2col3x3")
+    # col2im through the ReLU: channels a multiple of 4
+    refused(lib.splat_nn_col2im_act3x3(a, b, c, C.c_void_p(0x40000), 1, 8, 8, 6, 2, 56, None),
+            "col2im_act3x3")
+    # Adam over arrays: at most 16 segments, pointers of non-empty ones
+    segs = (_lib.SplatAdamSeg * 17)()
+    refused(lib.splat_nn_adam_multi(segs, 17, 1e-3, 1, None), "adam_multi")
+    one = (_lib.SplatAdamSeg * 1)(_lib.SplatAdamSeg(None, None, None, None, None, 10))
+    refused(lib.splat_nn_adam_multi(one, 1, 1e-3, 1, None), "adam_multi")
+    refused(lib.splat_nn_adam_multi(one, 1, 1e-3, 0, None), "adam_multi")  # step >= 1
